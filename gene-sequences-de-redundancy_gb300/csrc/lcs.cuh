@@ -1,0 +1,152 @@
+// lcs.cuh -- warp-cooperative bit-parallel LCS decision.
+//
+// Decides LCS(pattern, text) >= c over gap-free 2-bit packed sequences, the
+// test of the reference's kernel_align (cuda-version/func.cu:828-999, a full
+// O(q*T) DP per thread).  Here one warp evaluates one pair with Hyyro's
+// bit-vector recurrence over the pattern positions:
+//     U = V & M[c];  V' = (V + U) | (V & ~M[c]);   LCS = zeros of V
+// Lane l holds pattern words l*W .. l*W+W-1 (bit b of word w <-> position 32w+b),
+// so one text character advances 32*W*32 DP cells per warp step.  The carry of
+// the multi-word addition crosses lanes with a carry-lookahead on two ballots:
+// with G = lanes that generate a carry and P = lanes that propagate one, the
+// carry into lane l is bit l of ((G + (G|P)) ^ P).
+//
+// Match masks are built per step from two bit planes of the pattern (high and
+// low bit of each base): M[c] = ~((H ^ ch) | (L ^ cl)), ch/cl = the text
+// base's bits broadcast to all 32 positions.  Bits above the pattern length
+// never influence lower bits (carries only move up), so padding needs no mask
+// except when counting zeros.
+//
+// Early exits are exact: the LCS of the pattern with a text prefix never
+// decreases, so the pair is accepted as soon as it reaches c, and rejected as
+// soon as even matching every remaining text base could not reach c.
+#pragma once
+#include <stdint.h>
+
+namespace gsdr {
+
+__device__ __forceinline__ uint32_t even_bits(uint32_t x) {
+    x &= 0x55555555u;
+    x = (x | (x >> 1)) & 0x33333333u;
+    x = (x | (x >> 2)) & 0x0f0f0f0fu;
+    x = (x | (x >> 4)) & 0x00ff00ffu;
+    x = (x | (x >> 8)) & 0x0000ffffu;
+    return x;
+}
+
+// High / low bit planes of 32 bases held in two packed words (first base in
+// bits 31:30 of u0): bit b of the result belongs to base b.
+__device__ __forceinline__ void planes32(uint32_t u0, uint32_t u1, uint32_t& hi, uint32_t& lo) {
+    const uint32_t b0 = __brev(u0), b1 = __brev(u1);
+    hi = even_bits(b0) | (even_bits(b1) << 16);
+    lo = even_bits(b0 >> 1) | (even_bits(b1 >> 1) << 16);
+}
+
+__device__ __forceinline__ int warp_sum_i(int v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    return v;
+}
+
+// Returns true iff LCS(pattern, text) >= c.  pq: pattern packed words
+// (q bases); pt: text packed words (T bases).  Requires 1 <= c, q <= 1024*W.
+// STORE = keep the step's masks and sums in registers (small W) or recompute
+// them in a second pass (large W, fewer live registers).
+template <int W, bool STORE>
+__device__ bool lcs_reaches_warp(const uint32_t* __restrict__ pq, int q,
+                                 const uint32_t* __restrict__ pt, int T, int c, int lane) {
+    uint32_t H[W], Lo[W], V[W];
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        const int w = lane * W + i;
+        uint32_t hi = 0, lo = 0;
+        if (w * 32 < q) planes32(__ldg(pq + 2 * w), __ldg(pq + 2 * w + 1), hi, lo);
+        H[i] = hi;
+        Lo[i] = lo;
+        V[i] = 0xffffffffu;
+    }
+    const unsigned lane_bit = 1u << lane;
+    const int tw_count = (T + 15) >> 4;
+    int x = 0;
+    int zeros = 0;
+    while (x < T) {
+        // 32 text words (512 bases) per refill, one per lane.
+        const int wbase = x >> 4;
+        const uint32_t tw_lane = (wbase + lane < tw_count) ? __ldg(pt + wbase + lane) : 0u;
+        const int xend = min(T, x + 512);
+        while (x < xend) {
+            const uint32_t tw = __shfl_sync(0xffffffffu, tw_lane, (x >> 4) & 31);
+            const int bend = min(16, xend - x);
+            for (int b = 0; b < bend; b++, x++) {
+                const uint32_t cc = (tw >> (30 - 2 * b)) & 3u;
+                const uint32_t ch = 0u - (cc >> 1), cl = 0u - (cc & 1u);
+                if (STORE) {
+                    uint32_t m[W], s[W];
+                    uint32_t carry = 0, ones = 0xffffffffu;
+#pragma unroll
+                    for (int i = 0; i < W; i++) {
+                        m[i] = ~((H[i] ^ ch) | (Lo[i] ^ cl));
+                        const uint64_t t = (uint64_t)V[i] + (V[i] & m[i]) + carry;
+                        s[i] = (uint32_t)t;
+                        carry = (uint32_t)(t >> 32);
+                        ones &= s[i];
+                    }
+                    const unsigned G = __ballot_sync(0xffffffffu, carry != 0);
+                    const unsigned P = __ballot_sync(0xffffffffu, ones == 0xffffffffu);
+                    uint32_t cin = (((G + (G | P)) ^ P) & lane_bit) ? 1u : 0u;
+#pragma unroll
+                    for (int i = 0; i < W; i++) {
+                        const uint64_t t = (uint64_t)s[i] + cin;
+                        cin = (uint32_t)(t >> 32);
+                        V[i] = (uint32_t)t | (V[i] & ~m[i]);
+                    }
+                } else {
+                    uint32_t carry = 0, ones = 0xffffffffu;
+#pragma unroll
+                    for (int i = 0; i < W; i++) {
+                        const uint32_t m = ~((H[i] ^ ch) | (Lo[i] ^ cl));
+                        const uint64_t t = (uint64_t)V[i] + (V[i] & m) + carry;
+                        carry = (uint32_t)(t >> 32);
+                        ones &= (uint32_t)t;
+                    }
+                    const unsigned G = __ballot_sync(0xffffffffu, carry != 0);
+                    const unsigned P = __ballot_sync(0xffffffffu, ones == 0xffffffffu);
+                    uint32_t cin = (((G + (G | P)) ^ P) & lane_bit) ? 1u : 0u;
+#pragma unroll
+                    for (int i = 0; i < W; i++) {
+                        const uint32_t m = ~((H[i] ^ ch) | (Lo[i] ^ cl));
+                        const uint64_t t = (uint64_t)V[i] + (V[i] & m) + cin;
+                        cin = (uint32_t)(t >> 32);
+                        V[i] = (uint32_t)t | (V[i] & ~m);
+                    }
+                }
+                if ((x & 31) == 31) {
+                    int z = 0;
+#pragma unroll
+                    for (int i = 0; i < W; i++) {
+                        const int w = lane * W + i;
+                        const int rem = q - 32 * w;
+                        const uint32_t valid =
+                            rem >= 32 ? 0xffffffffu : (rem > 0 ? ((1u << rem) - 1u) : 0u);
+                        z += __popc(~V[i] & valid);
+                    }
+                    zeros = warp_sum_i(z);
+                    if (zeros >= c) return true;
+                    if (zeros + (T - 1 - x) < c) return false;
+                }
+            }
+        }
+    }
+    int z = 0;
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        const int w = lane * W + i;
+        const int rem = q - 32 * w;
+        const uint32_t valid = rem >= 32 ? 0xffffffffu : (rem > 0 ? ((1u << rem) - 1u) : 0u);
+        z += __popc(~V[i] & valid);
+    }
+    zeros = warp_sum_i(z);
+    return zeros >= c;
+}
+
+}  // namespace gsdr

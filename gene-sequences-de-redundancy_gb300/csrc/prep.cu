@@ -1,0 +1,234 @@
+// prep.cu -- one-time per-job preparation kernels.
+//
+// k_pack fuses the reference's kernel_baseToNumber, kernel_compressData,
+// kernel_createPrefix and kernel_createCutoff (cuda-version/func.cu:139-186,
+// 272-403, 312-349): one warp per read streams the raw bytes with aligned
+// 16-byte loads, drops non-ACGT bytes, packs 16 bases per u32 (first base in
+// the two most significant bits), counts the bases and computes the cutoffs
+// with the reference's float/double types.
+//
+// k_kmers_hist replaces kernel_createWords*/sortWords/mergeWords
+// (cuda-version/func.cu:405-653): instead of a per-thread Shell sort of every
+// k-mer, a CTA counts the read's k-mers in a shared-memory histogram and
+// emits one (k-mer, multiplicity) entry per distinct k-mer.  The word filter
+// only needs that multiset, not an order.
+#include <cuda_runtime.h>
+
+#include "gsdr_device.cuh"
+
+namespace gsdr {
+
+namespace {
+
+constexpr int kPackWarps = 8;
+
+__device__ __forceinline__ int base_code(uint32_t b) {
+    // A/a->0, C/c->1, G/g->2, T/t/U/u->3, anything else->4 (func.cu:139-179).
+    uint32_t l = b | 0x20u;
+    return l == 'a' ? 0 : l == 'c' ? 1 : l == 'g' ? 2 : (l == 't' || l == 'u') ? 3 : 4;
+}
+
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    return v;
+}
+
+// kernel_createCutoff (cuda-version/func.cu:312-337) with explicit rounding
+// intrinsics so that no contraction can change a result.
+__device__ void cutoffs(int length, float t, int k, int* word, int* base, int* pig) {
+    int required = length - k + 1;
+    double c1 = ceil(__dmul_rn((double)(float)length, __dsub_rn(1.0, (double)t)));
+    int cutoff = (int)__dmul_rn(c1, (double)k);
+    required -= cutoff;
+    required = max(required, 1);
+    float offset;
+    if ((double)t >= 0.9) {
+        offset = (float)__dsub_rn(1.1, __dmul_rn(fabs(__dsub_rn((double)t, 0.95)), 2.0));
+    } else {
+        offset = 1.0f;
+    }
+    *word = (int)ceilf(__fmul_rn((float)required, offset));
+    *base = (int)ceilf(__fmul_rn((float)length, t));
+    *pig = (int)__dmul_rn(c1, 4.0);
+}
+
+__global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, int k) {
+    __shared__ uint32_t stage_all[kPackWarps][36];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    uint32_t* stage = stage_all[wib];
+    const int nwarps = gridDim.x * kPackWarps;
+    for (int r = blockIdx.x * kPackWarps + wib; r < R.n; r += nwarps) {
+        const uint8_t* src = R.bytes + R.off[r];
+        const int L = R.len[r];
+        const uintptr_t start = (uintptr_t)src;
+        const uintptr_t a0 = start & ~(uintptr_t)15;
+        const int head = (int)(start - a0);
+        const long long nchunks = ((long long)head + L + 15) >> 4;
+        uint32_t* out = R.packed + R.pack_off[r];
+        for (int w = lane; w < 36; w += 32) stage[w] = 0;
+        __syncwarp();
+        int gcount = 0;
+        int cnt0 = 0, cnt1 = 0, cnt2 = 0, cnt3 = 0;
+        for (long long c0 = 0; c0 < nchunks; c0 += 32) {
+            const long long c = c0 + lane;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (c < nchunks) v = __ldcs(reinterpret_cast<const uint4*>(a0) + c);
+            const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+            int nb = 0;
+            uint32_t acc = 0;
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+                const long long pos = 16 * c + jj - head;
+                const bool valid = (c < nchunks) && pos >= 0 && pos < L;
+                const int code = valid ? base_code((words[jj >> 2] >> (8 * (jj & 3))) & 0xffu) : 4;
+                if (code < 4) {
+                    acc = (acc << 2) | (uint32_t)code;
+                    nb++;
+                    cnt0 += code == 0;
+                    cnt1 += code == 1;
+                    cnt2 += code == 2;
+                    cnt3 += code == 3;
+                }
+            }
+            acc = nb ? (acc << (2 * (16 - nb))) : 0u;
+            int incl = nb;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                int x = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += x;
+            }
+            const int excl = incl - nb;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int gpos = gcount + excl;
+            const int wrel = (gpos >> 4) - (gcount >> 4);
+            const int sh = gpos & 15;
+            if (nb) {
+                atomicOr(&stage[wrel], acc >> (2 * sh));
+                if (sh + nb > 16) atomicOr(&stage[wrel + 1], acc << (2 * (16 - sh)));
+            }
+            __syncwarp();
+            const int nfull = ((gcount + total) >> 4) - (gcount >> 4);
+            for (int w = lane; w < nfull; w += 32) out[(gcount >> 4) + w] = stage[w];
+            const uint32_t carry = stage[nfull];
+            __syncwarp();
+            for (int w = lane; w < 36; w += 32) stage[w] = 0;
+            __syncwarp();
+            if (lane == 0) stage[0] = carry;
+            __syncwarp();
+            gcount += total;
+        }
+        // kernel_compressData always stores the trailing (possibly empty) word.
+        if (lane == 0) out[gcount >> 4] = stage[0];
+        cnt0 = warp_sum(cnt0);
+        cnt1 = warp_sum(cnt1);
+        cnt2 = warp_sum(cnt2);
+        cnt3 = warp_sum(cnt3);
+        if (lane == 0) {
+            R.len_gf[r] = gcount;
+            R.comp[r] = make_int4(cnt0, cnt1, cnt2, cnt3);
+            int cw, cb, cp;
+            cutoffs(L, t, k, &cw, &cb, &cp);
+            R.cut_word[r] = cw;
+            R.cut_base[r] = cb;
+            R.cut_pig[r] = cp;
+        }
+        __syncwarp();
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
+    constexpr int NB = 1 << (2 * K);
+    extern __shared__ __align__(16) uint32_t sm[];
+    uint32_t* hist = sm;
+    uint16_t* list = reinterpret_cast<uint16_t*>(sm + NB);
+    __shared__ int nlist;
+    for (int i = threadIdx.x; i < NB; i += blockDim.x) hist[i] = 0;
+    if (threadIdx.x == 0) nlist = 0;
+    __syncthreads();
+    for (int r = blockIdx.x; r < R.n; r += gridDim.x) {
+        const int gf = R.len_gf[r];
+        const int nk = gf - K + 1;
+        uint32_t* out = R.kmer + R.kmer_off[r];
+        if (nk <= 0) {
+            if (threadIdx.x == 0) R.n_kmer[r] = 0;
+            continue;
+        }
+        const uint32_t* pk = R.packed + R.pack_off[r];
+        for (int p = threadIdx.x; p < nk; p += blockDim.x) {
+            const int w = p >> 4, o = p & 15;
+            const uint64_t v = ((uint64_t)__ldg(pk + w) << 32) | __ldg(pk + w + 1);
+            const uint32_t km = (uint32_t)(v >> (64 - 2 * o - 2 * K)) & (uint32_t)(NB - 1);
+            const uint32_t old = atomicAdd(&hist[km], 1u);
+            if (old == 0) list[atomicAdd(&nlist, 1)] = (uint16_t)km;
+        }
+        __syncthreads();
+        const int nl = nlist;
+        for (int s = threadIdx.x; s < nl; s += blockDim.x) {
+            const uint32_t km = list[s];
+            const uint32_t c = hist[km];
+            out[s] = (km << 16) | (c & 0xffffu);
+            hist[km] = 0;
+        }
+        const int padded = (nl + 3) & ~3;
+        for (int s = nl + threadIdx.x; s < padded; s += blockDim.x) out[s] = 0u;
+        if (threadIdx.x == 0) R.n_kmer[r] = nl;
+        __syncthreads();
+        if (threadIdx.x == 0) nlist = 0;
+        __syncthreads();
+    }
+}
+
+template <int K>
+int kmers_hist_launch(const DevReads& R, cudaStream_t s) {
+    constexpr int NB = 1 << (2 * K);
+    const int smem = NB * 4 + NB * 2;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_kmers_hist<K>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return 1;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_kmers_hist<K>, 256, smem);
+    if (per_sm < 1) per_sm = 1;
+    int grid = num_sms() * per_sm;
+    if (grid > R.n) grid = R.n > 0 ? R.n : 1;
+    k_kmers_hist<K><<<grid, 256, smem, s>>>(R);
+    return 0;
+}
+
+}  // namespace
+
+int num_sms() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+void launch_pack(const DevReads& R, float t, int k, cudaStream_t s) {
+    if (R.n <= 0) return;
+    int grid = (R.n + kPackWarps - 1) / kPackWarps;
+    const int cap = num_sms() * 16;
+    if (grid > cap) grid = cap;
+    k_pack<<<grid, kPackWarps * 32, 0, s>>>(R, t, k);
+}
+
+int launch_kmers(const DevReads& R, int k, cudaStream_t s) {
+    if (R.n <= 0) return 0;
+    switch (k) {
+        case 4: return kmers_hist_launch<4>(R, s);
+        case 5: return kmers_hist_launch<5>(R, s);
+        case 6: return kmers_hist_launch<6>(R, s);
+        case 7: return kmers_hist_launch<7>(R, s);
+        default: return 2;
+    }
+}
+
+}  // namespace gsdr

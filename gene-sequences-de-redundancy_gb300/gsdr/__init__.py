@@ -1,0 +1,330 @@
+"""Python view of the GB300 clustering library (ctypes over libgsdr.so).
+
+The names follow the reference program's functions (cuda-version/func.h):
+``check_option`` (checkOption), ``read_file`` (readFile), ``clustering``
+(clustering / clusteringDrop with the preparation kernels before them),
+``save_file`` (saveFile) and ``main``.  Everything runs through the C ABI
+declared in include/gsdr.h; there is no Python or CPU fallback: a missing
+library or CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BUILD_DIR = os.path.join(_PKG, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libgsdr.so")
+SYNTH_PATH = os.path.join(BUILD_DIR, "libgsdr_synth.so")
+CLI_PATH = os.path.join(BUILD_DIR, "cluster")
+
+OK, EINVAL, ENOMEM, EDEVICE, ETIMEOUT, EIO, EUNSUPPORTED, EBUSY, ENOTFOUND = range(9)
+
+
+class GsdrError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"gsdr status {status}: {msg}")
+        self.status = status
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("threshold", C.c_float),
+        ("word_length", C.c_int32),
+        ("drop", C.c_int32),
+        ("pigeon", C.c_int32),
+        ("batch", C.c_int32),
+        ("device", C.c_int32),
+        ("stage_timing", C.c_int32),
+        ("verbose", C.c_int32),
+    ]
+
+
+class Reads(C.Structure):
+    _fields_ = [
+        ("bytes", C.c_void_p),
+        ("n_bytes", C.c_int64),
+        ("offset", C.c_void_p),
+        ("length", C.c_void_p),
+        ("n", C.c_int32),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("rounds", C.c_int64),
+        ("passes", C.c_int64),
+        ("pairs_prefilter", C.c_int64),
+        ("pairs_word", C.c_int64),
+        ("pairs_aligned", C.c_int64),
+        ("pairs_accepted", C.c_int64),
+        ("cells", C.c_double),
+        ("filter_bytes", C.c_double),
+        ("ms_h2d", C.c_double),
+        ("ms_prep", C.c_double),
+        ("ms_cluster", C.c_double),
+        ("ms_d2h", C.c_double),
+        ("ms_total", C.c_double),
+        ("ms_filter", C.c_double),
+        ("ms_align", C.c_double),
+        ("k", C.c_int32),
+        ("drop", C.c_int32),
+        ("pigeon", C.c_int32),
+        ("batch", C.c_int32),
+        ("kernel_launches", C.c_int64),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("max_inflight", C.c_int32),
+        ("mem_budget", C.c_int64),
+        ("batch", C.c_int32),
+    ]
+
+
+class SynthCfg(C.Structure):
+    _fields_ = [
+        ("n_reads", C.c_int64),
+        ("n_seeds", C.c_int64),
+        ("len_dist", C.c_int32),
+        ("copies_max", C.c_int32),
+        ("len_lo", C.c_double),
+        ("len_hi", C.c_double),
+        ("len_median", C.c_double),
+        ("len_sigma", C.c_double),
+        ("id_lo", C.c_double),
+        ("sub_frac", C.c_double),
+        ("indel_lo", C.c_int32),
+        ("indel_hi", C.c_int32),
+        ("gc_lo", C.c_double),
+        ("gc_hi", C.c_double),
+        ("mode", C.c_int32),
+        ("pad_", C.c_int32),
+        ("extra_indel_frac", C.c_double),
+        ("seed", C.c_uint64),
+    ]
+
+
+_lib = None
+_synth = None
+
+
+def lib():
+    """Loads libgsdr.so (built by build.py); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise GsdrError(EDEVICE, f"{LIB_PATH} is not built; run the package build first")
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        L.gsdr_cluster.argtypes = [P(Reads), P(Opts), C.c_void_p, P(Stats)]
+        L.gsdr_fasta_read.argtypes = [C.c_char_p, P(C.c_void_p)]
+        L.gsdr_fasta_parse.argtypes = [C.c_char_p, C.c_int64, P(C.c_void_p)]
+        L.gsdr_fasta_count.argtypes = [C.c_void_p]
+        L.gsdr_fasta_view.argtypes = [C.c_void_p, P(Reads)]
+        L.gsdr_fasta_order.argtypes = [C.c_void_p]
+        L.gsdr_fasta_order.restype = C.c_void_p
+        L.gsdr_fasta_name.argtypes = [C.c_void_p, C.c_int32, P(C.c_int64)]
+        L.gsdr_fasta_name.restype = C.c_void_p
+        L.gsdr_fasta_write.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, P(C.c_int64)]
+        L.gsdr_fasta_format.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                        P(C.c_int64)]
+        L.gsdr_fasta_free.argtypes = [C.c_void_p]
+        L.gsdr_default_opts.argtypes = [P(Opts)]
+        L.gsdr_resolve_opts.argtypes = [P(Opts), P(C.c_char_p)]
+        L.gsdr_check_option.argtypes = [C.c_int, P(C.c_char_p), P(Opts), C.c_char_p,
+                                        C.c_char_p, C.c_int64]
+        L.gsdr_main.argtypes = [C.c_int, P(C.c_char_p)]
+        L.gsdr_strerror.restype = C.c_char_p
+        L.gsdr_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def synth_lib():
+    global _synth
+    if _synth is None:
+        if not os.path.exists(SYNTH_PATH):
+            raise GsdrError(EDEVICE, f"{SYNTH_PATH} is not built")
+        S = C.CDLL(SYNTH_PATH)
+        S.gsdr_synth_preset.argtypes = [C.c_int, C.POINTER(SynthCfg)]
+        S.gsdr_synth_generate.argtypes = [C.POINTER(SynthCfg), C.POINTER(C.c_void_p),
+                                          C.POINTER(C.c_int64)]
+        S.gsdr_synth_generate.restype = C.c_int64
+        S.gsdr_synth_write.argtypes = [C.POINTER(SynthCfg), C.c_char_p]
+        S.gsdr_synth_write.restype = C.c_int64
+        S.gsdr_synth_free.argtypes = [C.c_void_p]
+        _synth = S
+    return _synth
+
+
+def _check(status):
+    if status != OK:
+        msg = lib().gsdr_last_error().decode(errors="replace")
+        raise GsdrError(status, msg or lib().gsdr_strerror(status).decode())
+
+
+# ---- options -------------------------------------------------------------------
+
+def default_opts(**kw) -> Opts:
+    o = Opts()
+    lib().gsdr_default_opts(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def resolve_opts(o: Opts) -> Opts:
+    o2 = Opts.from_buffer_copy(o)
+    _check(lib().gsdr_resolve_opts(C.byref(o2), None))
+    return o2
+
+
+def check_option(argv):
+    """checkOption: argv without the program name.  Returns (opts, in, out)
+    or raises GsdrError(EINVAL) where the reference prints its usage."""
+    args = [b"cluster"] + [a.encode() if isinstance(a, str) else a for a in argv]
+    arr = (C.c_char_p * len(args))(*args)
+    o = Opts()
+    cap = 4096
+    ib, ob = C.create_string_buffer(cap), C.create_string_buffer(cap)
+    _check(lib().gsdr_check_option(len(args), arr, C.byref(o), ib, ob, cap))
+    return o, ib.value.decode(), ob.value.decode()
+
+
+# ---- FASTA ---------------------------------------------------------------------
+
+class Fasta:
+    """Reads parsed and sorted as readFile does; owns the native object."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+        self.n = lib().gsdr_fasta_count(self._h)
+        v = Reads()
+        _check(lib().gsdr_fasta_view(self._h, C.byref(v)))
+        self.view = v
+
+    @classmethod
+    def read(cls, path):
+        h = C.c_void_p()
+        _check(lib().gsdr_fasta_read(os.fsencode(path), C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def parse(cls, data: bytes):
+        h = C.c_void_p()
+        _check(lib().gsdr_fasta_parse(data, len(data), C.byref(h)))
+        return cls(h.value)
+
+    def order(self) -> np.ndarray:
+        p = lib().gsdr_fasta_order(self._h)
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_int32)), (self.n,)).copy()
+
+    def lengths(self) -> np.ndarray:
+        return np.ctypeslib.as_array(C.cast(self.view.length, C.POINTER(C.c_int32)),
+                                     (self.n,)).copy()
+
+    def format(self, cluster: np.ndarray) -> bytes:
+        cl = np.ascontiguousarray(cluster, dtype=np.int32)
+        need = C.c_int64()
+        _check(lib().gsdr_fasta_format(self._h, cl.ctypes.data, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(max(need.value, 1))
+        _check(lib().gsdr_fasta_format(self._h, cl.ctypes.data, buf, need.value, C.byref(need)))
+        return buf.raw[: need.value]
+
+    def write(self, path, cluster: np.ndarray) -> int:
+        cl = np.ascontiguousarray(cluster, dtype=np.int32)
+        n = C.c_int64()
+        _check(lib().gsdr_fasta_write(os.fsencode(path), self._h, cl.ctypes.data, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if self._h:
+            lib().gsdr_fasta_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def read_file(path) -> Fasta:
+    """readFile (cuda-version/func.cu:94-117)."""
+    return Fasta.read(path)
+
+
+def save_file(path, fasta: Fasta, cluster) -> int:
+    """saveFile (cuda-version/func.cu:1099-1111); returns the cluster count."""
+    return fasta.write(path, cluster)
+
+
+# ---- clustering ----------------------------------------------------------------
+
+def clustering(fasta: Fasta, opts: Opts | None = None, stats: bool = False, **kw):
+    """The device path (cuda-version/func.cu:119-1097): returns cluster[] in
+    sorted order (and the Stats when stats=True)."""
+    o = opts if opts is not None else default_opts()
+    if kw:
+        o = Opts.from_buffer_copy(o)
+        for k, v in kw.items():
+            setattr(o, k, v)
+    cl = np.empty(max(fasta.n, 1), dtype=np.int32)
+    st = Stats()
+    _check(lib().gsdr_cluster(C.byref(fasta.view), C.byref(o), cl.ctypes.data, C.byref(st)))
+    cl = cl[: fasta.n]
+    return (cl, st) if stats else cl
+
+
+def cluster_bytes(data: bytes, **kw) -> bytes:
+    """FASTA bytes in, representative FASTA bytes out (one call)."""
+    f = Fasta.parse(data)
+    try:
+        cl = clustering(f, **kw)
+        return f.format(cl)
+    finally:
+        f.close()
+
+
+def main(argv) -> int:
+    """main (cuda-version/main.cu:3-36)."""
+    args = [b"cluster"] + [a.encode() if isinstance(a, str) else a for a in argv]
+    arr = (C.c_char_p * len(args))(*args)
+    return lib().gsdr_main(len(args), arr)
+
+
+# ---- synthetic workloads ---------------------------------------------------------
+
+def synth_config(config: int, n_reads: int | None = None, seed: int | None = None,
+                 **kw) -> SynthCfg:
+    c = SynthCfg()
+    synth_lib().gsdr_synth_preset(config, C.byref(c))
+    if n_reads is not None and n_reads != c.n_reads:
+        c.n_seeds = max(1, int(round(c.n_seeds * n_reads / c.n_reads)))
+        c.n_reads = n_reads
+    if seed is not None:
+        c.seed = seed
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def synth_fasta(config: int, n_reads: int | None = None, seed: int | None = None, **kw) -> bytes:
+    c = synth_config(config, n_reads, seed, **kw)
+    p = C.c_void_p()
+    n = C.c_int64()
+    r = synth_lib().gsdr_synth_generate(C.byref(c), C.byref(p), C.byref(n))
+    if r < 0:
+        raise GsdrError(EINVAL, f"synthetic generator failed ({r})")
+    try:
+        return C.string_at(p.value, n.value)
+    finally:
+        synth_lib().gsdr_synth_free(p)

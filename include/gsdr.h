@@ -1,0 +1,163 @@
+/* gsdr.h -- C ABI of the GB300 greedy exact-identity clustering library.
+ *
+ * The reference program (JuZhenCS/gene-sequences-de-redundancy, cuda-version)
+ * has no library interface: main() calls free functions in a fixed order
+ * (cuda-version/main.cu:3-36).  Each entry point below replaces one of those
+ * functions, with the same argument meaning, and returns a status code where
+ * the reference printed a message and exited.  Plain pointers and sizes only.
+ *
+ *   gsdr_check_option   <- checkOption        cuda-version/func.cu:10-92
+ *   gsdr_fasta_read     <- readFile           cuda-version/func.cu:94-117
+ *   gsdr_cluster        <- copyData .. mergeWords, clustering / clusteringDrop
+ *                          cuda-version/func.cu:119-653, 1001-1097
+ *                          (the declarations in cuda-version/func.h:55-77)
+ *   gsdr_fasta_write    <- saveFile           cuda-version/func.cu:1099-1111
+ *   gsdr_main           <- main               cuda-version/main.cu:3-36
+ *
+ * A representative is the longest still-unclustered read; every later
+ * unclustered read whose gap-free LCS with it reaches ceil(len * t) (after the
+ * reference's base-composition prefilter, optional pigeon filter and k-mer
+ * word filter) joins it.  Results are bit-identical to the reference.
+ */
+#ifndef GSDR_H
+#define GSDR_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define GSDR_OK 0
+#define GSDR_EINVAL 1       /* bad argument; the reference prints usage and exits (func.cu:4-8,43-84) */
+#define GSDR_ENOMEM 2       /* host or device allocation failed */
+#define GSDR_EDEVICE 3      /* CUDA error, no usable device, or missing CUDA code */
+#define GSDR_ETIMEOUT 4     /* a bounded device-side wait gave up */
+#define GSDR_EIO 5          /* file could not be written */
+#define GSDR_EUNSUPPORTED 6 /* input outside what this build handles (message says which) */
+#define GSDR_EBUSY 7        /* serving: queue full */
+#define GSDR_ENOTFOUND 8    /* serving: unknown job id */
+
+/* Options, as struct Option (cuda-version/func.h:9-16) plus execution knobs. */
+typedef struct {
+    float threshold;      /* t: 0.8 <= t < 1 (func.cu:43) */
+    int32_t word_length;  /* k: 0 = derive from t as func.cu:49-58 does; else 4..12 */
+    int32_t drop;         /* 0 = filters on, 1 = alignment only, 3 = derive from t (func.cu:67-72) */
+    int32_t pigeon;       /* 0 or 1: the 4-mer position filter (func.cu:756-801) */
+    int32_t batch;        /* tentative representatives per pass: 1 = one per round
+                             (the reference's form); >1 = batched; 0 = automatic */
+    int32_t device;       /* CUDA device ordinal */
+    int32_t stage_timing; /* 1: time each stage with CUDA events (slower; for profiling) */
+    int32_t verbose;      /* 1: print the reference's progress lines to stdout */
+} gsdr_opts;
+
+/* Reads in length-sorted order (the order readFile leaves them in).  Read i is
+ * bytes[offset[i] .. offset[i] + length[i]) -- verbatim sequence bytes, any
+ * letters; bytes outside A/C/G/T/U (either case) are gaps (func.cu:139-179). */
+typedef struct {
+    const char* bytes;
+    int64_t n_bytes;
+    const int64_t* offset;
+    const int32_t* length;
+    int32_t n;
+} gsdr_reads;
+
+typedef struct {
+    int64_t rounds;           /* representatives taken (one per round in the plain form) */
+    int64_t passes;           /* device passes (batched: one per batch of tentatives) */
+    int64_t pairs_prefilter;  /* (representative, candidate) pairs that reached the prefilter */
+    int64_t pairs_word;       /* pairs that reached the word filter */
+    int64_t pairs_aligned;    /* pairs that reached the alignment */
+    int64_t pairs_accepted;
+    double cells;             /* sum over aligned pairs of gap-free q x T (full-DP cells) */
+    double filter_bytes;      /* bytes the filter stage streamed (algorithmic) */
+    double ms_h2d, ms_prep, ms_cluster, ms_d2h, ms_total;
+    double ms_filter, ms_align; /* with stage_timing only */
+    int32_t k, drop, pigeon, batch;
+    int64_t kernel_launches;  /* kernels launched by the library during the call */
+} gsdr_stats;
+
+/* Fill `o` with the reference defaults (t 0.95, derived k/drop, pigeon 0). */
+void gsdr_default_opts(gsdr_opts* o);
+
+/* Derive k and drop from t exactly as checkOption does and validate ranges.
+ * Returns GSDR_OK or GSDR_EINVAL (with a message in *msg if msg != NULL). */
+int gsdr_resolve_opts(gsdr_opts* o, const char** msg);
+
+/* checkOption (cuda-version/func.cu:10-92): argv holds letter/value pairs
+ * i o t w d p; only the first character of a key counts, and a leading '-'
+ * is also accepted.  Paths are copied into in_path/out_path (cap bytes each).
+ * Returns GSDR_OK or GSDR_EINVAL (the reference's usage exit). */
+int gsdr_check_option(int argc, char** argv, gsdr_opts* o, char* in_path, char* out_path,
+                      int64_t cap);
+
+/* readFile (cuda-version/func.cu:94-117).  Parses the FASTA file with the
+ * reference's getline rules and sorts reads longest first with the same
+ * std::sort call, so that ties come out in the same order.  An unreadable
+ * file behaves like an empty one, as in the reference. */
+typedef struct gsdr_fasta gsdr_fasta;
+int gsdr_fasta_read(const char* path, gsdr_fasta** out);
+/* Same, from a buffer already in memory (copied). */
+int gsdr_fasta_parse(const char* data, int64_t n, gsdr_fasta** out);
+int32_t gsdr_fasta_count(const gsdr_fasta* f);
+/* View of the sorted reads (valid while f lives). */
+int gsdr_fasta_view(const gsdr_fasta* f, gsdr_reads* view);
+/* order[i] = file position of sorted read i (n entries, valid while f lives). */
+const int32_t* gsdr_fasta_order(const gsdr_fasta* f);
+/* Name line (verbatim, with its '>') of sorted read i. */
+const char* gsdr_fasta_name(const gsdr_fasta* f, int32_t i, int64_t* len);
+/* saveFile (cuda-version/func.cu:1099-1111): for each sorted read i with
+ * cluster[i] == i write "name\n" and "sequence\n". */
+int gsdr_fasta_write(const char* path, const gsdr_fasta* f, const int32_t* cluster,
+                     int64_t* n_written);
+/* The same bytes into a caller buffer; returns the size needed in *need. */
+int gsdr_fasta_format(const gsdr_fasta* f, const int32_t* cluster, char* buf, int64_t cap,
+                      int64_t* need);
+void gsdr_fasta_free(gsdr_fasta* f);
+
+/* The clustering path (cuda-version/func.cu:119-653 preparation and the loop
+ * of func.cu:1001-1097).  cluster[i] receives the representative of sorted
+ * read i (cluster[i] == i for representatives).  Host buffers in and out;
+ * device memory is managed by the library.  `stats` may be NULL. */
+int gsdr_cluster(const gsdr_reads* reads, const gsdr_opts* opts, int32_t* cluster,
+                 gsdr_stats* stats);
+
+/* main (cuda-version/main.cu:3-36): the `cluster` command line.  Returns the
+ * process exit status (0 also for the usage exit, as in the reference). */
+int gsdr_main(int argc, char** argv);
+
+const char* gsdr_strerror(int status);
+/* Text of the last error on this thread (more detail than gsdr_strerror). */
+const char* gsdr_last_error(void);
+
+/* ---- Serving: continuous batching of independent clustering jobs ----------
+ * No counterpart in the reference.  Jobs are admitted by device-memory
+ * footprint, run concurrently on separate CUDA streams, and each job's result
+ * equals what gsdr_cluster returns for it alone. */
+typedef struct gsdr_server gsdr_server;
+typedef struct {
+    int32_t device;
+    int32_t max_inflight;     /* concurrent jobs on the device (streams) */
+    int64_t mem_budget;       /* device bytes for job data; 0 = 80% of free memory */
+    int32_t batch;            /* as gsdr_opts.batch */
+} gsdr_server_opts;
+int gsdr_server_create(const gsdr_server_opts* so, gsdr_server** out);
+/* Submit a job: the FASTA bytes are copied; t as in gsdr_opts.  Returns the
+ * job id in *job. */
+int gsdr_server_submit(gsdr_server* s, const char* fasta, int64_t n, float threshold,
+                       int64_t* job);
+/* Wait up to timeout_ms (-1 = forever) for a finished job; returns its id,
+ * status and timing.  GSDR_ETIMEOUT when none finished in time. */
+int gsdr_server_wait(gsdr_server* s, int64_t timeout_ms, int64_t* job, int32_t* job_status,
+                     double* latency_ms);
+/* Result of a finished job: representative FASTA bytes (caller buffer; *need
+ * receives the size) and the cluster array in sorted order (may be NULL). */
+int gsdr_server_result(gsdr_server* s, int64_t job, char* buf, int64_t cap, int64_t* need,
+                       int32_t* cluster, int32_t* n_reads);
+int gsdr_server_release(gsdr_server* s, int64_t job);
+void gsdr_server_destroy(gsdr_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

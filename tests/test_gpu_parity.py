@@ -1,0 +1,136 @@
+"""GPU path vs the oracle: cluster arrays and FASTA bytes must be identical.
+
+All cases are integer work, so the tolerance is zero.  Inputs are seeded
+synthetic workloads (the reference's own input file is not distributed) and
+hand-made edge cases.
+"""
+import numpy as np
+import pytest
+
+import gsdr
+import oracle_binding as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(data: bytes, tmp_path, t=0.95, w=0, d=3, p=0, batch=1):
+    order, ocl, ost, ofa = orc.run_bytes(data, tmp_path, t=t, w=w, d=d, p=p)
+    f = gsdr.Fasta.parse(data)
+    assert f.n == len(ocl)
+    np.testing.assert_array_equal(f.order(), order)
+    cl, st = gsdr.clustering(f, gsdr.default_opts(threshold=t, word_length=w, drop=d, pigeon=p,
+                                                  batch=batch), stats=True)
+    out = f.format(cl)
+    f.close()
+    return cl, ocl, out, ofa, st, ost
+
+
+def assert_same(cl, ocl, out, ofa):
+    bad = np.nonzero(cl != ocl)[0]
+    assert len(bad) == 0, f"{len(bad)} reads differ, first {bad[:10]}: gpu {cl[bad[:10]]} oracle {ocl[bad[:10]]}"
+    assert out == ofa
+
+
+@pytest.mark.parametrize("n,seed", [(600, 1), (3000, 2)])
+def test_c0_recipe(tmp_path, n, seed):
+    data = gsdr.synth_fasta(0, n_reads=n, seed=seed)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95)
+    assert_same(cl, ocl, out, ofa)
+    assert st.rounds == ost.rounds
+    assert st.pairs_accepted == ost.accepted
+
+
+def test_c0_full(tmp_path):
+    data = gsdr.synth_fasta(0)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95)
+    assert_same(cl, ocl, out, ofa)
+    assert st.pairs_word == ost.prefilter_pass
+    assert st.pairs_aligned == ost.aligned
+
+
+@pytest.mark.parametrize("t", [0.88, 0.90, 0.93, 0.97, 0.99])
+def test_thresholds_word_lengths(tmp_path, t):
+    data = gsdr.synth_fasta(0, n_reads=2000, seed=11)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=t)
+    assert st.k == ost.k
+    assert_same(cl, ocl, out, ofa)
+
+
+@pytest.mark.parametrize("w", [4, 5, 6, 7])
+def test_word_length_override(tmp_path, w):
+    data = gsdr.synth_fasta(0, n_reads=1500, seed=5)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95, w=w)
+    assert_same(cl, ocl, out, ofa)
+
+
+@pytest.mark.parametrize("t", [0.80, 0.85])
+def test_drop_mode(tmp_path, t):
+    data = gsdr.synth_fasta(0, n_reads=700, seed=3)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=t)
+    assert ost.drop == 1 and st.drop == 1
+    assert_same(cl, ocl, out, ofa)
+
+
+def test_drop_forced_at_high_t(tmp_path):
+    data = gsdr.synth_fasta(0, n_reads=600, seed=4)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95, d=1)
+    assert_same(cl, ocl, out, ofa)
+
+
+def test_c1_recipe_slice(tmp_path):
+    data = gsdr.synth_fasta(1, n_reads=20000, seed=21)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95)
+    assert_same(cl, ocl, out, ofa)
+    assert st.cells == ost.cells
+
+
+def test_c2_recipe_slice(tmp_path):
+    # all reads 150 bp: the order is pure std::sort tie-breaking
+    data = gsdr.synth_fasta(2, n_reads=30000, seed=31)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.90)
+    assert_same(cl, ocl, out, ofa)
+
+
+def test_c3_recipe_slice_drop(tmp_path):
+    data = gsdr.synth_fasta(3, n_reads=120, seed=41)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.80)
+    assert_same(cl, ocl, out, ofa)
+
+
+def _mixed_edge_fasta(seed=9):
+    rng = np.random.default_rng(seed)
+    recs = []
+    base = rng.choice(list(b"ACGT"), 700).tobytes()
+    for i in range(60):
+        s = bytearray(base[: rng.integers(150, 700)])
+        for _ in range(rng.integers(0, 12)):
+            s[rng.integers(0, len(s))] = rng.choice(list(b"ACGTNRYacgtnu"))
+        if i % 7 == 0:
+            s += b"\r"
+        recs.append(b">r%d desc\n" % i + bytes(s) + b"\n")
+    recs.append(b">short1\nACG\n")
+    recs.append(b">short2\nACGTA\n")
+    recs.append(b">multiline\n" + base[:100] + b"\n" + base[100:300] + b"\n\n" + base[300:400] + b"\n")
+    recs.append(b">dup1\n" + base[:500] + b"\n")
+    recs.append(b">dup2\n" + base[:500] + b"\n")
+    return b"".join(recs)
+
+
+@pytest.mark.parametrize("t", [0.95, 0.90, 0.85])
+def test_edge_symbols_and_layout(tmp_path, t):
+    data = _mixed_edge_fasta()
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=t)
+    assert_same(cl, ocl, out, ofa)
+
+
+def test_all_n_read_drop_mode(tmp_path):
+    data = b">a\n" + b"ACGT" * 50 + b"\n>n\n" + b"N" * 300 + b"\n>b\n" + b"ACGT" * 40 + b"\n>e\n\n"
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.85)
+    assert_same(cl, ocl, out, ofa)
+
+
+def test_single_read_and_no_newline(tmp_path):
+    data = b">only\nACGTACGTAC"
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95)
+    assert_same(cl, ocl, out, ofa)
+    assert out == b">only\nACGTACGTAC\n"

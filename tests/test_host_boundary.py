@@ -1,0 +1,84 @@
+"""Host side of the boundary (no GPU): FASTA reading with the reference's
+line rules and std::sort tie order, the writer, and option parsing, each
+against the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+import gsdr
+import oracle_binding as orc
+
+
+def oracle_fasta_roundtrip(data, tmp_path):
+    """Oracle output when every read is its own representative (t=0.99 on
+    unrelated random reads keeps them all), to compare the writer bytes."""
+    order, cl, st, fa = orc.run_bytes(data, tmp_path, t=0.99, d=1)
+    return order, cl, fa
+
+
+def test_tie_order_matches_std_sort(tmp_path):
+    rng = np.random.default_rng(0)
+    lens = rng.choice([50, 51, 52, 60], size=3000)
+    recs = [b">x%d\n" % i + rng.choice(list(b"ACGT"), int(L)).tobytes() + b"\n"
+            for i, L in enumerate(lens)]
+    data = b"".join(recs)
+    path = tmp_path / "ties.fa"
+    path.write_bytes(data)
+    order, _, _ = orc.run(str(path), None, t=0.99, d=1, max_rounds=0)
+    f = gsdr.read_file(str(path))
+    np.testing.assert_array_equal(f.order(), order)
+    # same permutation as a plain stable sort would NOT give in general
+    stable = np.argsort(-lens, kind="stable")
+    assert not np.array_equal(stable, order)
+
+
+@pytest.mark.parametrize("data", [
+    b"",
+    b"ACGT\n>a\nAC\n",
+    b">a\nAC\r\nGT\r\n>b\r\nA\n",
+    b">a\n\n\nACGT\n\n>b\nAAAA",
+    b">only",
+    b"\n>a\nACGT\n",
+    b">a\nAC\nGT\nNN\n>b\nACG\n>c\n",
+])
+def test_reader_layout_cases(tmp_path, data):
+    path = tmp_path / "in.fa"
+    path.write_bytes(data)
+    order, cl, st = orc.run(str(path), str(tmp_path / "o.fa"), t=0.99, d=1)
+    f = gsdr.read_file(str(path))
+    np.testing.assert_array_equal(f.order(), order)
+    out = f.format(cl)
+    assert out == (tmp_path / "o.fa").read_bytes()
+
+
+def test_missing_file_reads_as_empty(tmp_path):
+    f = gsdr.read_file(str(tmp_path / "does_not_exist.fa"))
+    assert f.n == 1
+    assert f.format(np.array([0], dtype=np.int32)) == b"\n\n"
+
+
+@pytest.mark.parametrize("argv", [
+    ["t", "0.95"], ["t", "0.88"], ["t", "0.879"], ["t", "0.8"], ["t", "0.94"], ["t", "0.97"],
+    ["t", "0.9", "w", "9"], ["t", "0.9", "d", "1"], ["t", "0.85", "d", "0"], ["p", "1"],
+    ["t", "1.0"], ["t", "0.79"], ["w", "3"], ["w", "13"], ["d", "2"], ["p", "2"], ["x", "1"],
+    ["t"], ["i", "a.fa", "o", "b.fa", "t", "0.91"],
+])
+def test_check_option_matches(argv):
+    ref = orc.check_option(argv)
+    try:
+        o, _, _ = gsdr.check_option(argv)
+        got = (o.threshold, o.word_length, o.drop, o.pigeon)
+    except gsdr.GsdrError as e:
+        assert e.status == gsdr.EINVAL
+        got = None
+    if ref is None:
+        assert got is None
+    else:
+        assert got is not None
+        assert np.float32(got[0]) == np.float32(ref[0]) and got[1:] == ref[1:]
+
+
+def test_dash_spelling_accepted():
+    o, i, out = gsdr.check_option(["-t", "0.9", "--i", "x.fa", "-o", "y.fa"])
+    assert abs(o.threshold - 0.9) < 1e-7 and i == "x.fa" and out == "y.fa" and o.word_length == 7
