@@ -1,0 +1,317 @@
+"""Benchmark: greedy exact-identity clustering of the 200k-read workload
+(lognormal lengths, median 1500 bp, 40k seeds, t = 0.95) on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config 1] [--batch R]
+
+One step = one full clustering of the workload (preparation kernels + every
+round).  Prints one JSON line.
+  value      sequences/s with the reads already in HBM (gsdr_job_run, CUDA
+             events on the job's stream);
+  e2e        sequences/s through gsdr_cluster with host buffers (H2D of the
+             sequence bytes and D2H of the cluster array inside the timing);
+  roofline   the filter stage (dominant HBM stream) from a stage-timed run;
+  cpu_baseline  the oracle (CPU restatement of the reference path) on the
+             host cores, on the same workload.
+--impl reference times the oracle alone (the reference has no CPU path of its
+own) and prints its line.  Under torchrun each rank clusters an independent
+replica (the path keeps one GPU per job), rank 0 prints.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gene-sequences-de-redundancy_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+CONFIG_NAMES = {
+    0: "10k reads, 200-1000 bp, t=0.95",
+    1: "200k reads, lognormal median 1500 bp sigma 0.5 (300-10000), 40k seeds, t=0.95",
+    2: "2M reads of 150 bp, 300k seeds, t=0.90",
+    3: "300k reads, log-uniform 2-30 kbp, 60k seeds, t=0.80",
+}
+CONFIG_T = {0: 0.95, 1: 0.95, 2: 0.90, 3: 0.80}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        loaded = [x for x in sm if smax and x > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def oracle_lib():
+    import oracle_binding
+
+    oracle_binding.build()
+    return oracle_binding
+
+
+def cpu_run(data_path, t, threads):
+    orc = oracle_lib()
+    t0 = time.perf_counter()
+    order, cl, st = orc.run(data_path, None, t=t, threads=threads)
+    dt = time.perf_counter() - t0
+    return dt, len(cl), st
+
+
+def write_workload(cfg, n_reads, seed, path):
+    import gsdr
+
+    c = gsdr.synth_config(cfg, n_reads, seed)
+    n = gsdr.synth_lib().gsdr_synth_write(c, os.fsencode(path))
+    if n < 0:
+        raise RuntimeError("workload generation failed")
+    return n
+
+
+def bench_reference(args, rank, world):
+    """--impl reference: the oracle (CPU restatement) on the host cores."""
+    if rank != 0:
+        return None
+    import gsdr  # noqa: F401  (generator)
+
+    threads = os.cpu_count() or 1
+    path = os.path.join("/tmp", f"gsdr_bench_c{args.config}_{os.getpid()}.fa")
+    n = write_workload(args.config, args.reads, args.seed, path)
+    t = CONFIG_T[args.config]
+    times = []
+    for i in range(args.warmup + args.steps):
+        dt, nr, st = cpu_run(path, t, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    os.unlink(path)
+    sec = sum(times) / len(times)
+    value = n / sec
+    return {
+        "metric": "seqs/sec", "value": value, "unit": "seqs/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": CONFIG_NAMES[args.config], "reads": n, "threshold": t,
+                   "l2": "host run"},
+        "cpu_baseline": {"value": value, "unit": "seqs/s", "cores": threads, "kind": "port",
+                         "sample": f"whole workload ({n} reads) per step; the reference has "
+                                   "no CPU path, so its restatement (oracle) runs"},
+        "e2e": {"value": value, "unit": "seqs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def bench_ours(args, rank, world, local):
+    import gsdr
+
+    device = local if world > 1 else 0
+    data = gsdr.synth_fasta(args.config, args.reads, args.seed)
+    t = CONFIG_T[args.config]
+    f = gsdr.Fasta.parse(data)
+    n = f.n
+    opts = gsdr.default_opts(threshold=t, device=device, batch=args.batch)
+    h2d = f.view.n_bytes + n * 8 + n * 4 + 2 * (n + 1) * 8
+    d2h = n * 4
+
+    # value: device-resident input
+    job = gsdr.Job(f, opts)
+    for _ in range(args.warmup):
+        job.run()
+    clocks = ClockSampler(device)
+    clocks.start()
+    dev_ms = []
+    launches = 0
+    last = None
+    for _ in range(args.steps):
+        st = job.run()
+        dev_ms.append(st.ms_prep + st.ms_cluster)
+        launches += st.kernel_launches
+        last = st
+    clock_info = clocks.stop()
+    cl_dev = job.cluster()
+    job.close()
+
+    # e2e: host buffers through gsdr_cluster
+    for _ in range(min(args.warmup, 2)):
+        gsdr.clustering(f, opts)
+    e2e_ms = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cl = gsdr.clustering(f, opts)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    same = bool((cl == cl_dev).all())
+
+    # stage-timed run for the roofline (events around each filter / align launch)
+    st_t = gsdr.clustering(f, gsdr.default_opts(threshold=t, device=device, batch=args.batch,
+                                                stage_timing=1), stats=True)[1]
+    f.close()
+
+    dev_ms_max = max(dev_ms)  # max over steps of this rank; max over ranks below
+    ms_step = sum(dev_ms) / len(dev_ms)
+    e2e_step = sum(e2e_ms) / len(e2e_ms)
+    peak, peak_kind = measured_peaks()
+    filt_gbs = st_t.filter_bytes / (st_t.ms_filter * 1e-3) / 1e9 if st_t.ms_filter > 0 else 0.0
+    align_gcups = st_t.cells / (st_t.ms_align * 1e-3) / 1e9 if st_t.ms_align > 0 else 0.0
+    return {
+        "n": n, "ms_step": ms_step, "ms_step_max": dev_ms_max, "e2e_ms": e2e_step,
+        "h2d": h2d, "d2h": d2h, "launches_per_step": launches // max(1, args.steps),
+        "stats": last.as_dict(), "clocks": clock_info, "same": same,
+        "filter_gbs": filt_gbs, "filter_ms": st_t.ms_filter, "filter_bytes": st_t.filter_bytes,
+        "filter_launches": st_t.rounds, "align_ms": st_t.ms_align, "gcups": align_gcups,
+        "peak": peak, "peak_kind": peak_kind, "t": t,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--reads", type=int, default=None)
+    ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        line = bench_reference(args, rank, world)
+        if world > 1:
+            dist.barrier()
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    if world > 1:
+        dist.barrier()
+    r = bench_ours(args, rank, world, local)
+    if world > 1:
+        import torch
+
+        t = torch.tensor([r["ms_step"], r["e2e_ms"]], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        r["ms_step"], r["e2e_ms"] = float(t[0]), float(t[1])
+        dist.barrier()
+    if rank != 0:
+        return
+    n_total = r["n"] * world
+    value = n_total / (r["ms_step"] * 1e-3)
+    e2e = n_total / (r["e2e_ms"] * 1e-3)
+    line = {
+        "metric": "seqs/sec", "value": value, "unit": "seqs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic",
+        "config": {"workload": CONFIG_NAMES[args.config], "reads": r["n"], "threshold": r["t"],
+                   "form": "plain" if args.batch == 1 else f"batched R={args.batch}",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (sequence bytes + k-mer tables > 1 GB per step)"},
+        "e2e": {"value": e2e, "unit": "seqs/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
+        "gpu_launches": r["launches_per_step"] * args.steps,
+        "clocks": r["clocks"],
+        "roofline": {"bound": "hbm", "kernel": "k_filter (prefilter + word filter)",
+                     "achieved": r["filter_gbs"], "peak": r["peak"], "unit": "GB/s",
+                     "frac": r["filter_gbs"] / r["peak"] if r["peak"] else None,
+                     "peak_source": r["peak_kind"], "traffic": None,
+                     "stage_ms": r["filter_ms"], "bytes": r["filter_bytes"]},
+        "align": {"gcups": r["gcups"], "stage_ms": r["align_ms"],
+                  "cells": r["stats"]["cells"]},
+        "stats": {k: r["stats"][k] for k in ("rounds", "passes", "pairs_prefilter", "pairs_word",
+                                               "pairs_aligned", "pairs_accepted", "ms_prep",
+                                               "ms_cluster")},
+        "device_result_matches_e2e": r["same"],
+    }
+    if not args.no_cpu:
+        import tempfile
+
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "w.fa")
+            n = write_workload(args.config, args.reads, args.seed, path)
+            threads = os.cpu_count() or 1
+            dt, _, _ = cpu_run(path, r["t"], threads)
+        line["cpu_baseline"] = {"value": n / dt, "unit": "seqs/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"whole workload ({n} reads), one run"}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,17 +1,20 @@
-// api.cu -- the C ABI: gsdr_cluster (the reference's copyData .. clustering
-// sequence, cuda-version/main.cu:9-30) and gsdr_main (the CLI).
+// api.cu -- the C ABI around gsdr::Job: gsdr_cluster (the reference's
+// copyData .. clustering sequence, cuda-version/main.cu:9-30), the job entry
+// points, and gsdr_main (the CLI).
 #include <cuda_runtime.h>
 
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
 #include "gsdr.h"
 #include "gsdr_device.cuh"
 #include "gsdr_host.h"
+#include "job.h"
 
 namespace gsdr {
 
@@ -31,25 +34,20 @@ double now_ms() {
 
 namespace {
 
-#define GSDR_CUDA(call)                                                             \
-    do {                                                                            \
-        cudaError_t e_ = (call);                                                    \
-        if (e_ != cudaSuccess) {                                                    \
-            std::string m_ = std::string(#call) + ": " + cudaGetErrorString(e_);    \
-            rc = fail(e_ == cudaErrorMemoryAllocation ? GSDR_ENOMEM : GSDR_EDEVICE, \
-                      m_.c_str());                                                  \
-            goto done;                                                              \
-        }                                                                           \
-    } while (0)
-
 inline int64_t round4(int64_t v) { return (v + 3) & ~(int64_t)3; }
 
-// All device buffers of one clustering call, in one allocation.
-struct JobMem {
-    void* base = nullptr;
-    size_t bytes = 0;
-};
+int cuda_fail(cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(e == cudaErrorMemoryAllocation ? GSDR_ENOMEM : GSDR_EDEVICE, m.c_str());
+}
 
+#define JCUDA(call)                                   \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+// Sub-allocations of one device allocation, each 256-byte aligned.
 struct Carve {
     char* p;
     size_t used = 0;
@@ -61,10 +59,296 @@ struct Carve {
     }
 };
 
+// Layout plan shared by footprint() and plan_and_alloc().
+struct Plan {
+    std::vector<int64_t> pack_off, kmer_off;
+    int64_t max_len = 0;
+};
+
+int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
+    const int n = reads->n;
+    const bool drop = o.drop == 1;
+    const int k = o.word_length;
+    P.pack_off.assign(n + 1, 0);
+    P.kmer_off.assign(n + 1, 0);
+    const int64_t kcap = (int64_t)1 << (2 * (k > 0 ? k : 1));
+    for (int i = 0; i < n; i++) {
+        const int64_t L = reads->length[i];
+        if (L < 0) return fail(GSDR_EINVAL, "negative read length");
+        if (reads->offset[i] < 0 || reads->offset[i] + L > reads->n_bytes)
+            return fail(GSDR_EINVAL, "read outside the byte buffer");
+        if (L > P.max_len) P.max_len = L;
+        P.pack_off[i + 1] = P.pack_off[i] + round4(L / 16 + 1);
+        int64_t ents = drop ? 0 : L - k + 1;
+        if (ents < 0) ents = 0;
+        if (ents > kcap) ents = kcap;
+        P.kmer_off[i + 1] = P.kmer_off[i] + round4(ents);
+    }
+    return GSDR_OK;
+}
+
+size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, int k, DevReads& R,
+                 RoundBuffers& B) {
+    Carve c{base};
+    R.n = n;
+    R.k = drop ? 0 : k;
+    R.bytes = c.take<uint8_t>((size_t)n_bytes + 64);
+    R.off = c.take<int64_t>(n);
+    R.len = c.take<int32_t>(n);
+    R.len_gf = c.take<int32_t>(n);
+    R.pack_off = c.take<int64_t>(n + 1);
+    R.packed = c.take<uint32_t>((size_t)P.pack_off[n] + 8);
+    R.comp = c.take<int4>(n);
+    R.cut_word = c.take<int32_t>(n);
+    R.cut_base = c.take<int32_t>(n);
+    R.cut_pig = c.take<int32_t>(n);
+    R.kmer_off = c.take<int64_t>(n + 1);
+    R.n_kmer = c.take<int32_t>(n);
+    R.kmer = c.take<uint32_t>((size_t)P.kmer_off[n] + 8);
+    B.st = reinterpret_cast<RoundState*>(c.take<char>(sizeof(RoundState) + 64));
+    B.cluster = c.take<int32_t>(n);
+    B.remain[0] = c.take<int32_t>(n);
+    B.remain[1] = c.take<int32_t>(n);
+    B.pair_cap = 2 * n;
+    B.pairs = c.take<Pair>((size_t)B.pair_cap);
+    return c.used + 256;
+}
+
+int validate(const gsdr_reads* reads, const gsdr_opts* opts_in, gsdr_opts& o) {
+    if (!reads || !opts_in) return fail(GSDR_EINVAL, "null argument");
+    if (reads->n < 0) return fail(GSDR_EINVAL, "negative read count");
+    if (reads->n > 0 && (!reads->offset || !reads->length || (!reads->bytes && reads->n_bytes)))
+        return fail(GSDR_EINVAL, "null read arrays");
+    o = *opts_in;
+    int rc = gsdr_resolve_opts(&o, nullptr);
+    if (rc) return rc;
+    if (o.drop == 0 && o.word_length > 7)
+        return fail(GSDR_EUNSUPPORTED, "word length above 7 is not built yet");
+    if (o.pigeon == 1 && o.drop == 0)
+        return fail(GSDR_EUNSUPPORTED, "the pigeon filter is not built yet");
+    return GSDR_OK;
+}
+
 }  // namespace
+
+Job::~Job() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (gexec_) cudaGraphExecDestroy(gexec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    for (auto& e : ev_)
+        if (e) cudaEventDestroy(e);
+    if (dmem_) cudaFree(dmem_);
+    if (h_done_) cudaFreeHost(h_done_);
+    if (h_state_) cudaFreeHost(h_state_);
+    if (own_stream_ && stream) cudaStreamDestroy(stream);
+}
+
+int64_t Job::footprint(const gsdr_reads* reads, const gsdr_opts* opts) {
+    gsdr_opts o;
+    if (validate(reads, opts, o)) return -1;
+    Plan P;
+    if (make_plan(reads, o, P)) return -1;
+    DevReads R{};
+    RoundBuffers B{};
+    return (int64_t)carve_all(nullptr, reads->n, reads->n_bytes, P, o.drop == 1, o.word_length,
+                              R, B);
+}
+
+int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s) {
+    int rc = validate(reads, opts_in, opts);
+    if (rc) return rc;
+    n = reads->n;
+    n_bytes_ = reads->n_bytes;
+    std::memset(&stats, 0, sizeof(stats));
+    stats.k = opts.word_length;
+    stats.drop = opts.drop;
+    stats.pigeon = opts.pigeon;
+    stats.batch = 1;
+    Plan P;
+    rc = make_plan(reads, opts, P);
+    if (rc) return rc;
+    if (P.max_len > 32 * kMaxPatternWords)
+        return fail(GSDR_EUNSUPPORTED, "reads above 32768 bases are not built yet");
+    pack_off_.swap(P.pack_off);
+    kmer_off_.swap(P.kmer_off);
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
+        return fail(GSDR_EDEVICE, "no CUDA device");
+    if (opts.device < 0 || opts.device >= dev_count) return fail(GSDR_EINVAL, "bad device");
+    JCUDA(cudaSetDevice(opts.device));
+    if (s) {
+        stream = s;
+    } else {
+        JCUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream_ = true;
+    }
+    for (auto& e : ev_) JCUDA(cudaEventCreate(&e));
+    JCUDA(cudaMallocHost(&h_done_, sizeof(int32_t)));
+    JCUDA(cudaMallocHost(&h_state_, sizeof(RoundState)));
+    if (n == 0) return GSDR_OK;
+    Plan P2;
+    P2.pack_off = pack_off_;
+    P2.kmer_off = kmer_off_;
+    dbytes_ = carve_all(nullptr, n, n_bytes_, P2, opts.drop == 1, opts.word_length, R_, B_);
+    JCUDA(cudaMalloc(&dmem_, dbytes_));
+    carve_all(reinterpret_cast<char*>(dmem_), n, n_bytes_, P2, opts.drop == 1, opts.word_length,
+              R_, B_);
+    return GSDR_OK;
+}
+
+int Job::upload(const gsdr_reads* reads) {
+    if (n == 0) return GSDR_OK;
+    JCUDA(cudaEventRecord(ev_[0], stream));
+    JCUDA(cudaMemcpyAsync((void*)R_.bytes, reads->bytes, (size_t)reads->n_bytes,
+                          cudaMemcpyHostToDevice, stream));
+    JCUDA(cudaMemcpyAsync((void*)R_.off, reads->offset, sizeof(int64_t) * n,
+                          cudaMemcpyHostToDevice, stream));
+    JCUDA(cudaMemcpyAsync((void*)R_.len, reads->length, sizeof(int32_t) * n,
+                          cudaMemcpyHostToDevice, stream));
+    JCUDA(cudaMemcpyAsync((void*)R_.pack_off, pack_off_.data(), sizeof(int64_t) * (n + 1),
+                          cudaMemcpyHostToDevice, stream));
+    JCUDA(cudaMemcpyAsync((void*)R_.kmer_off, kmer_off_.data(), sizeof(int64_t) * (n + 1),
+                          cudaMemcpyHostToDevice, stream));
+    JCUDA(cudaEventRecord(ev_[1], stream));
+    JCUDA(cudaStreamSynchronize(stream));  // host buffers may be released after upload
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+    stats.ms_h2d = ms;
+    return GSDR_OK;
+}
+
+int Job::capture_graph() {
+    if (gexec_) return GSDR_OK;
+    const int unroll = 16;  // rounds per graph launch; even, so the remain buffers alternate
+    JCUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed));
+    long long per = 0;
+    for (int r = 0; r < unroll; r++)
+        launch_plain_round(R_, B_, opts.threshold, opts.drop, opts.pigeon, r & 1, stream, &per,
+                           nullptr);
+    cudaError_t e = cudaStreamEndCapture(stream, &graph_);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    JCUDA(cudaGraphInstantiate(&gexec_, graph_, 0));
+    graph_launches_per_ = per;
+    return GSDR_OK;
+}
+
+int Job::loop_graph() {
+    int rc = capture_graph();
+    if (rc) return rc;
+    while (true) {
+        JCUDA(cudaGraphLaunch(gexec_, stream));
+        stats.kernel_launches += graph_launches_per_;
+        JCUDA(cudaMemcpyAsync(h_done_, &B_.st->done, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                              stream));
+        JCUDA(cudaStreamSynchronize(stream));
+        if (*h_done_) break;
+    }
+    return GSDR_OK;
+}
+
+int Job::loop_timed() {
+    cudaEvent_t e4[4] = {};
+    for (auto& e : e4) JCUDA(cudaEventCreate(&e));
+    int parity = 0;
+    double fms = 0, ams = 0;
+    long long launches = 0;
+    int rc = GSDR_OK;
+    while (true) {
+        launch_plain_round(R_, B_, opts.threshold, opts.drop, opts.pigeon, parity, stream,
+                           &launches, e4);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h_done_, &B_.st->done, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "timed round");
+            break;
+        }
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, e4[0], e4[1]);
+        cudaEventElapsedTime(&b, e4[1], e4[2]);
+        fms += a;
+        ams += b;
+        parity ^= 1;
+        if (*h_done_) break;
+    }
+    stats.ms_filter = fms;
+    stats.ms_align = ams;
+    stats.kernel_launches += launches;
+    for (auto& e : e4) cudaEventDestroy(e);
+    return rc;
+}
+
+int Job::run() {
+    if (n == 0) return GSDR_OK;
+    const double t0 = now_ms();
+    const int k = opts.word_length;
+    const bool drop = opts.drop == 1;
+    stats.kernel_launches = 0;
+    JCUDA(cudaSetDevice(opts.device));
+    JCUDA(cudaEventRecord(ev_[1], stream));
+    // baseToNumber + compressData + createCutoff + createPrefix (func.cu:139-403)
+    JCUDA(cudaMemsetAsync(R_.packed, 0, sizeof(uint32_t) * ((size_t)pack_off_[n] + 8), stream));
+    launch_pack(R_, opts.threshold, k, stream);
+    stats.kernel_launches += 1;
+    JCUDA(cudaGetLastError());
+    // createWords + sortWords + mergeWords (func.cu:405-653)
+    if (!drop) {
+        if (launch_kmers(R_, k, stream)) return fail(GSDR_EDEVICE, "k-mer kernel configuration");
+        stats.kernel_launches += 1;
+        JCUDA(cudaGetLastError());
+    }
+    JCUDA(cudaEventRecord(ev_[2], stream));
+    // clustering / clusteringDrop (func.cu:1001-1097)
+    init_rounds(R_, B_, stream);
+    stats.kernel_launches += 1;
+    JCUDA(cudaGetLastError());
+    int rc = opts.stage_timing ? loop_timed() : loop_graph();
+    if (rc) return rc;
+    JCUDA(cudaEventRecord(ev_[3], stream));
+    JCUDA(cudaMemcpyAsync(h_state_, B_.st, sizeof(RoundState), cudaMemcpyDeviceToHost, stream));
+    JCUDA(cudaStreamSynchronize(stream));
+    JCUDA(cudaGetLastError());
+    if (h_state_->pair_overflow) return fail(GSDR_EDEVICE, "alignment queue overflow");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev_[1], ev_[2]);
+    stats.ms_prep = ms;
+    cudaEventElapsedTime(&ms, ev_[2], ev_[3]);
+    stats.ms_cluster = ms;
+    const RoundState& h = *h_state_;
+    stats.rounds = h.rounds;
+    stats.passes = h.passes;
+    stats.pairs_prefilter = (int64_t)h.cnt_prefilter;
+    stats.pairs_word = (int64_t)h.cnt_word;
+    stats.pairs_aligned = (int64_t)h.cnt_aligned;
+    stats.pairs_accepted = (int64_t)h.cnt_accepted;
+    stats.cells = (double)h.cells;
+    stats.filter_bytes = (double)h.filter_bytes;
+    stats.ms_total = now_ms() - t0;
+    return GSDR_OK;
+}
+
+int Job::download(int32_t* cluster) {
+    if (n == 0) return GSDR_OK;
+    JCUDA(cudaEventRecord(ev_[4], stream));
+    JCUDA(cudaMemcpyAsync(cluster, B_.cluster, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                          stream));
+    JCUDA(cudaEventRecord(ev_[5], stream));
+    JCUDA(cudaStreamSynchronize(stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev_[4], ev_[5]);
+    stats.ms_d2h = ms;
+    return GSDR_OK;
+}
+
 }  // namespace gsdr
 
 using namespace gsdr;
+
+struct gsdr_job {
+    Job job;
+};
 
 extern "C" {
 
@@ -85,220 +369,47 @@ const char* gsdr_strerror(int s) {
 
 const char* gsdr_last_error(void) { return g_last_error.c_str(); }
 
-int gsdr_cluster(const gsdr_reads* reads, const gsdr_opts* opts_in, int32_t* cluster,
+int gsdr_job_create(const gsdr_reads* reads, const gsdr_opts* opts, gsdr_job** out) {
+    if (!out) return fail(GSDR_EINVAL, "null output");
+    *out = nullptr;
+    gsdr_job* j = new (std::nothrow) gsdr_job();
+    if (!j) return fail(GSDR_ENOMEM, "out of host memory");
+    int rc = j->job.init(reads, opts);
+    if (!rc) rc = j->job.upload(reads);
+    if (rc) {
+        delete j;
+        return rc;
+    }
+    *out = j;
+    return GSDR_OK;
+}
+
+int gsdr_job_run(gsdr_job* j, gsdr_stats* stats) {
+    if (!j) return fail(GSDR_EINVAL, "null job");
+    int rc = j->job.run();
+    if (stats) *stats = j->job.stats;
+    return rc;
+}
+
+int gsdr_job_cluster(gsdr_job* j, int32_t* cluster) {
+    if (!j || (!cluster && j->job.n > 0)) return fail(GSDR_EINVAL, "null argument");
+    return j->job.download(cluster);
+}
+
+void gsdr_job_free(gsdr_job* j) { delete j; }
+
+int gsdr_cluster(const gsdr_reads* reads, const gsdr_opts* opts, int32_t* cluster,
                  gsdr_stats* stats) {
-    if (!reads || !opts_in || (!cluster && reads->n > 0))
+    if (!reads || !opts || (!cluster && reads->n > 0))
         return fail(GSDR_EINVAL, "gsdr_cluster: null argument");
-    gsdr_opts o = *opts_in;
-    int rc = gsdr_resolve_opts(&o, nullptr);
-    if (rc) return rc;
-    const int n = reads->n;
-    if (n < 0) return fail(GSDR_EINVAL, "gsdr_cluster: negative read count");
-    gsdr_stats st_local;
-    gsdr_stats& S = stats ? *stats : st_local;
-    std::memset(&S, 0, sizeof(S));
-    S.k = o.word_length;
-    S.drop = o.drop;
-    S.pigeon = o.pigeon;
-    S.batch = 1;
-    if (n == 0) return GSDR_OK;
-    const int k = o.word_length;
-    const bool drop = o.drop == 1;
-    if (!drop && k > 7)
-        return fail(GSDR_EUNSUPPORTED, "gsdr_cluster: word length above 7 is not built yet");
-    if (o.pigeon == 1 && !drop)
-        return fail(GSDR_EUNSUPPORTED, "gsdr_cluster: pigeon filter is not built yet");
-
-    const double t_begin = now_ms();
-    // Host-side layout: word and entry offsets from the raw lengths.
-    std::vector<int64_t> pack_off(n + 1), kmer_off(n + 1);
-    int64_t max_len = 0;
-    pack_off[0] = 0;
-    kmer_off[0] = 0;
-    const int64_t kcap = (int64_t)1 << (2 * (k > 0 ? k : 1));
-    for (int i = 0; i < n; i++) {
-        const int64_t L = reads->length[i];
-        if (L < 0) return fail(GSDR_EINVAL, "gsdr_cluster: negative length");
-        if (reads->offset[i] < 0 || reads->offset[i] + L > reads->n_bytes)
-            return fail(GSDR_EINVAL, "gsdr_cluster: read outside the byte buffer");
-        if (L > max_len) max_len = L;
-        pack_off[i + 1] = pack_off[i] + round4(L / 16 + 1);
-        int64_t ents = drop ? 0 : L - k + 1;
-        if (ents < 0) ents = 0;
-        if (ents > kcap) ents = kcap;
-        kmer_off[i + 1] = kmer_off[i] + round4(ents);
-    }
-    if (max_len > 32 * kMaxPatternWords)
-        return fail(GSDR_EUNSUPPORTED, "gsdr_cluster: reads above 32768 bases are not built yet");
-
-    int dev_count = 0;
-    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
-        return fail(GSDR_EDEVICE, "gsdr_cluster: no CUDA device");
-    if (o.device < 0 || o.device >= dev_count) return fail(GSDR_EINVAL, "gsdr_cluster: bad device");
-
-    cudaStream_t s = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    cudaEvent_t ev[8] = {};
-    int32_t* h_done = nullptr;
-    RoundState* h_state = nullptr;
-    void* dmem = nullptr;
-    long long launches = 0;
-    DevReads R = {};
-    RoundBuffers B = {};
-    {
-        // Carve every buffer out of one allocation.
-        Carve c{nullptr};
-        auto plan = [&](Carve& cv) {
-            R.n = n;
-            R.k = drop ? 0 : k;
-            R.bytes = cv.take<uint8_t>((size_t)reads->n_bytes + 64);
-            R.off = cv.take<int64_t>(n);
-            R.len = cv.take<int32_t>(n);
-            R.len_gf = cv.take<int32_t>(n);
-            R.pack_off = cv.take<int64_t>(n + 1);
-            R.packed = cv.take<uint32_t>((size_t)pack_off[n] + 8);
-            R.comp = cv.take<int4>(n);
-            R.cut_word = cv.take<int32_t>(n);
-            R.cut_base = cv.take<int32_t>(n);
-            R.cut_pig = cv.take<int32_t>(n);
-            R.kmer_off = cv.take<int64_t>(n + 1);
-            R.n_kmer = cv.take<int32_t>(n);
-            R.kmer = cv.take<uint32_t>((size_t)kmer_off[n] + 8);
-            B.st = reinterpret_cast<RoundState*>(cv.take<char>(sizeof(RoundState) + 64));
-            B.cluster = cv.take<int32_t>(n);
-            B.remain[0] = cv.take<int32_t>(n);
-            B.remain[1] = cv.take<int32_t>(n);
-            B.pair_cap = 2 * n;
-            B.pairs = cv.take<Pair>((size_t)B.pair_cap);
-        };
-        plan(c);
-        const size_t total = c.used + 256;
-        GSDR_CUDA(cudaSetDevice(o.device));
-        GSDR_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-        GSDR_CUDA(cudaMalloc(&dmem, total));
-        Carve c2{reinterpret_cast<char*>(dmem)};
-        plan(c2);
-        GSDR_CUDA(cudaMallocHost(&h_done, sizeof(int32_t)));
-        GSDR_CUDA(cudaMallocHost(&h_state, sizeof(RoundState)));
-        for (auto& e : ev) GSDR_CUDA(cudaEventCreate(&e));
-
-        // ---- copyData (func.cu:119-137): one H2D copy of the sequence bytes.
-        GSDR_CUDA(cudaEventRecord(ev[0], s));
-        GSDR_CUDA(cudaMemcpyAsync((void*)R.bytes, reads->bytes, (size_t)reads->n_bytes,
-                                  cudaMemcpyHostToDevice, s));
-        GSDR_CUDA(cudaMemcpyAsync((void*)R.off, reads->offset, sizeof(int64_t) * n,
-                                  cudaMemcpyHostToDevice, s));
-        GSDR_CUDA(cudaMemcpyAsync((void*)R.len, reads->length, sizeof(int32_t) * n,
-                                  cudaMemcpyHostToDevice, s));
-        GSDR_CUDA(cudaMemcpyAsync((void*)R.pack_off, pack_off.data(), sizeof(int64_t) * (n + 1),
-                                  cudaMemcpyHostToDevice, s));
-        GSDR_CUDA(cudaMemcpyAsync((void*)R.kmer_off, kmer_off.data(), sizeof(int64_t) * (n + 1),
-                                  cudaMemcpyHostToDevice, s));
-        GSDR_CUDA(cudaEventRecord(ev[1], s));
-
-        // ---- baseToNumber + compressData + createCutoff + createPrefix
-        GSDR_CUDA(cudaMemsetAsync(R.packed, 0, sizeof(uint32_t) * ((size_t)pack_off[n] + 8), s));
-        launch_pack(R, o.threshold, k, s);
-        launches += 1;
-        GSDR_CUDA(cudaGetLastError());
-        // ---- createWords + sortWords + mergeWords
-        if (!drop) {
-            int krc = launch_kmers(R, k, s);
-            if (krc) {
-                rc = fail(GSDR_EDEVICE, "k-mer kernel configuration failed");
-                goto done;
-            }
-            launches += 1;
-            GSDR_CUDA(cudaGetLastError());
-        }
-        GSDR_CUDA(cudaEventRecord(ev[2], s));
-
-        // ---- clustering / clusteringDrop (func.cu:1001-1097)
-        init_rounds(R, B, s);
-        launches += 1;
-        GSDR_CUDA(cudaGetLastError());
-        if (o.stage_timing) {
-            cudaEvent_t e4[4];
-            for (auto& e : e4) GSDR_CUDA(cudaEventCreate(&e));
-            int parity = 0;
-            double fms = 0, ams = 0;
-            while (true) {
-                launch_plain_round(R, B, o.threshold, drop, o.pigeon, parity, s, &launches, e4);
-                GSDR_CUDA(cudaGetLastError());
-                GSDR_CUDA(cudaMemcpyAsync(h_done, &B.st->done, sizeof(int32_t),
-                                          cudaMemcpyDeviceToHost, s));
-                GSDR_CUDA(cudaStreamSynchronize(s));
-                float a = 0, b = 0;
-                cudaEventElapsedTime(&a, e4[0], e4[1]);
-                cudaEventElapsedTime(&b, e4[1], e4[2]);
-                fms += a;
-                ams += b;
-                parity ^= 1;
-                if (*h_done) break;
-            }
-            S.ms_filter = fms;
-            S.ms_align = ams;
-            for (auto& e : e4) cudaEventDestroy(e);
-        } else {
-            const int unroll = 16;  // rounds per graph launch (even: remain buffers alternate)
-            GSDR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-            long long per_graph = 0;
-            for (int r = 0; r < unroll; r++)
-                launch_plain_round(R, B, o.threshold, drop, o.pigeon, r & 1, s, &per_graph,
-                                   nullptr);
-            GSDR_CUDA(cudaStreamEndCapture(s, &graph));
-            GSDR_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
-            while (true) {
-                GSDR_CUDA(cudaGraphLaunch(gexec, s));
-                launches += per_graph;
-                GSDR_CUDA(cudaMemcpyAsync(h_done, &B.st->done, sizeof(int32_t),
-                                          cudaMemcpyDeviceToHost, s));
-                GSDR_CUDA(cudaStreamSynchronize(s));
-                if (*h_done) break;
-            }
-        }
-        GSDR_CUDA(cudaEventRecord(ev[3], s));
-        GSDR_CUDA(cudaMemcpyAsync(cluster, B.cluster, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
-                                  s));
-        GSDR_CUDA(cudaMemcpyAsync(h_state, B.st, sizeof(RoundState), cudaMemcpyDeviceToHost, s));
-        GSDR_CUDA(cudaEventRecord(ev[4], s));
-        GSDR_CUDA(cudaStreamSynchronize(s));
-        GSDR_CUDA(cudaGetLastError());
-        if (h_state->pair_overflow) {
-            rc = fail(GSDR_EDEVICE, "alignment queue overflow");
-            goto done;
-        }
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ev[0], ev[1]);
-        S.ms_h2d = ms;
-        cudaEventElapsedTime(&ms, ev[1], ev[2]);
-        S.ms_prep = ms;
-        cudaEventElapsedTime(&ms, ev[2], ev[3]);
-        S.ms_cluster = ms;
-        cudaEventElapsedTime(&ms, ev[3], ev[4]);
-        S.ms_d2h = ms;
-        S.rounds = h_state->rounds;
-        S.passes = h_state->passes;
-        S.pairs_prefilter = (int64_t)h_state->cnt_prefilter;
-        S.pairs_word = (int64_t)h_state->cnt_word;
-        S.pairs_aligned = (int64_t)h_state->cnt_aligned;
-        S.pairs_accepted = (int64_t)h_state->cnt_accepted;
-        S.cells = (double)h_state->cells;
-        S.filter_bytes = (double)h_state->filter_bytes;
-        S.kernel_launches = launches;
-        rc = GSDR_OK;
-    }
-done:
-    if (gexec) cudaGraphExecDestroy(gexec);
-    if (graph) cudaGraphDestroy(graph);
-    for (auto& e : ev)
-        if (e) cudaEventDestroy(e);
-    if (dmem) cudaFree(dmem);
-    if (h_done) cudaFreeHost(h_done);
-    if (h_state) cudaFreeHost(h_state);
-    if (s) cudaStreamDestroy(s);
-    S.ms_total = now_ms() - t_begin;
+    const double t0 = now_ms();
+    Job job;
+    int rc = job.init(reads, opts);
+    if (!rc) rc = job.upload(reads);
+    if (!rc) rc = job.run();
+    if (!rc) rc = job.download(cluster);
+    job.stats.ms_total = now_ms() - t0;
+    if (stats) *stats = job.stats;
     return rc;
 }
 

@@ -1,0 +1,55 @@
+// job.h -- one clustering job on one device: its device buffers, stream and
+// round-loop graph.  gsdr_cluster, the job entry points and the serving loop
+// all drive this object.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "gsdr.h"
+#include "gsdr_device.cuh"
+
+namespace gsdr {
+
+class Job {
+public:
+    ~Job();
+    // Validates options and sizes, allocates device memory, creates the stream.
+    int init(const gsdr_reads* reads, const gsdr_opts* opts, cudaStream_t stream = nullptr);
+    // Host -> device copy of the reads (asynchronous on the job's stream).
+    int upload(const gsdr_reads* reads);
+    // Preparation kernels + the round loop; the cluster array stays on device.
+    int run();
+    // Device -> host copy of the cluster array (synchronous).
+    int download(int32_t* cluster);
+    // Device bytes this job needs for its inputs (admission by footprint).
+    static int64_t footprint(const gsdr_reads* reads, const gsdr_opts* opts);
+
+    gsdr_opts opts{};
+    gsdr_stats stats{};
+    int n = 0;
+    cudaStream_t stream = nullptr;
+
+private:
+    int plan_and_alloc();
+    int capture_graph();
+    int loop_graph();
+    int loop_timed();
+
+    bool own_stream_ = false;
+    int64_t n_bytes_ = 0;
+    std::vector<int64_t> pack_off_, kmer_off_;
+    void* dmem_ = nullptr;
+    size_t dbytes_ = 0;
+    int32_t* h_done_ = nullptr;
+    RoundState* h_state_ = nullptr;
+    cudaEvent_t ev_[6] = {};
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t gexec_ = nullptr;
+    long long graph_launches_per_ = 0;
+    DevReads R_{};
+    RoundBuffers B_{};
+};
+
+}  // namespace gsdr

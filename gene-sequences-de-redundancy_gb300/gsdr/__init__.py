@@ -142,6 +142,10 @@ def lib():
         L.gsdr_check_option.argtypes = [C.c_int, P(C.c_char_p), P(Opts), C.c_char_p,
                                         C.c_char_p, C.c_int64]
         L.gsdr_main.argtypes = [C.c_int, P(C.c_char_p)]
+        L.gsdr_job_create.argtypes = [P(Reads), P(Opts), P(C.c_void_p)]
+        L.gsdr_job_run.argtypes = [C.c_void_p, P(Stats)]
+        L.gsdr_job_cluster.argtypes = [C.c_void_p, C.c_void_p]
+        L.gsdr_job_free.argtypes = [C.c_void_p]
         L.gsdr_strerror.restype = C.c_char_p
         L.gsdr_last_error.restype = C.c_char_p
         _lib = L
@@ -282,6 +286,38 @@ def clustering(fasta: Fasta, opts: Opts | None = None, stats: bool = False, **kw
     _check(lib().gsdr_cluster(C.byref(fasta.view), C.byref(o), cl.ctypes.data, C.byref(st)))
     cl = cl[: fasta.n]
     return (cl, st) if stats else cl
+
+
+class Job:
+    """A clustering job whose reads stay on the device (gsdr_job_*)."""
+
+    def __init__(self, fasta: Fasta, opts: Opts):
+        self.fasta = fasta
+        self.n = fasta.n
+        h = C.c_void_p()
+        _check(lib().gsdr_job_create(C.byref(fasta.view), C.byref(opts), C.byref(h)))
+        self._h = h
+
+    def run(self) -> Stats:
+        st = Stats()
+        _check(lib().gsdr_job_run(self._h, C.byref(st)))
+        return st
+
+    def cluster(self) -> np.ndarray:
+        cl = np.empty(max(self.n, 1), dtype=np.int32)
+        _check(lib().gsdr_job_cluster(self._h, cl.ctypes.data))
+        return cl[: self.n]
+
+    def close(self):
+        if self._h:
+            lib().gsdr_job_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def cluster_bytes(data: bytes, **kw) -> bytes:

@@ -122,6 +122,20 @@ void gsdr_fasta_free(gsdr_fasta* f);
 int gsdr_cluster(const gsdr_reads* reads, const gsdr_opts* opts, int32_t* cluster,
                  gsdr_stats* stats);
 
+/* The same path in three steps, for callers that keep a job's data on the
+ * device between calls (and for timing the device part alone):
+ *   gsdr_job_create  copyData (func.cu:119-137): device allocation + H2D copy
+ *   gsdr_job_run     preparation kernels and the round loop (func.cu:139-653,
+ *                    1001-1097) on the device-resident reads
+ *   gsdr_job_cluster the cluster array back to the host
+ * gsdr_job_run may be called again on the same job; it recomputes from the
+ * uploaded reads. */
+typedef struct gsdr_job gsdr_job;
+int gsdr_job_create(const gsdr_reads* reads, const gsdr_opts* opts, gsdr_job** out);
+int gsdr_job_run(gsdr_job* job, gsdr_stats* stats);
+int gsdr_job_cluster(gsdr_job* job, int32_t* cluster);
+void gsdr_job_free(gsdr_job* job);
+
 /* main (cuda-version/main.cu:3-36): the `cluster` command line.  Returns the
  * process exit status (0 also for the usage exit, as in the reference). */
 int gsdr_main(int argc, char** argv);
