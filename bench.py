@@ -239,7 +239,7 @@ def main():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--reads", type=int, default=None)
     ap.add_argument("--seed", type=int, default=None)
-    ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--batch", type=int, default=0, help="0 = batched, adaptive R up to 256; 1 = plain")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     rank, world, local = dist_env()

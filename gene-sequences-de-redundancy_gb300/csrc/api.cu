@@ -105,12 +105,20 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     R.kmer_off = c.take<int64_t>(n + 1);
     R.n_kmer = c.take<int32_t>(n);
     R.kmer = c.take<uint32_t>((size_t)P.kmer_off[n] + 8);
-    B.st = reinterpret_cast<RoundState*>(c.take<char>(sizeof(RoundState) + 64));
+    B.st = reinterpret_cast<RoundState*>(c.take<char>(sizeof(RoundState) + 4 * 64));
     B.cluster = c.take<int32_t>(n);
     B.remain[0] = c.take<int32_t>(n);
     B.remain[1] = c.take<int32_t>(n);
-    B.pair_cap = 2 * n;
-    B.pairs = c.take<Pair>((size_t)B.pair_cap);
+    B.seg_cap = n > (1 << 16) ? n : (1 << 16);
+    B.pairs = c.take<Pair>((size_t)B.seg_cap * kAlignClasses);
+    B.tent = c.take<int32_t>(kMaxBatch);
+    B.tidx = c.take<uint32_t>(n);
+    B.best = c.take<uint32_t>(n);
+    B.tt = c.take<uint32_t>((size_t)kMaxBatch * kTTWords);
+    B.ttrow = c.take<uint32_t>(kTTWords);
+    B.survive = c.take<uint32_t>(kTTWords);
+    B.acc_cap = 2 * B.seg_cap;
+    B.acc = c.take<Pair>((size_t)B.acc_cap);
     return c.used + 256;
 }
 
@@ -163,7 +171,9 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     stats.k = opts.word_length;
     stats.drop = opts.drop;
     stats.pigeon = opts.pigeon;
-    stats.batch = 1;
+    batched_ = opts.batch != 1;
+    r_max_ = opts.batch == 0 ? 256 : (opts.batch > kMaxBatch ? kMaxBatch : opts.batch);
+    stats.batch = batched_ ? r_max_ : 1;
     Plan P;
     rc = make_plan(reads, opts, P);
     if (rc) return rc;
@@ -217,14 +227,18 @@ int Job::upload(const gsdr_reads* reads) {
     return GSDR_OK;
 }
 
+// One round (plain) or one pass (batched) of the device loop.
+void Job::launch_step(int parity, long long* count, cudaEvent_t* ev4) {
+    if (batched_) launch_batch_pass(R_, B_, opts.drop, parity, stream, count, ev4);
+    else launch_plain_round(R_, B_, opts.drop, parity, stream, count, ev4);
+}
+
 int Job::capture_graph() {
     if (gexec_) return GSDR_OK;
-    const int unroll = 16;  // rounds per graph launch; even, so the remain buffers alternate
+    const int unroll = batched_ ? 4 : 16;  // steps per graph launch; even, so the remain buffers alternate
     JCUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed));
     long long per = 0;
-    for (int r = 0; r < unroll; r++)
-        launch_plain_round(R_, B_, opts.threshold, opts.drop, opts.pigeon, r & 1, stream, &per,
-                           nullptr);
+    for (int r = 0; r < unroll; r++) launch_step(r & 1, &per, nullptr);
     cudaError_t e = cudaStreamEndCapture(stream, &graph_);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
     JCUDA(cudaGraphInstantiate(&gexec_, graph_, 0));
@@ -254,8 +268,7 @@ int Job::loop_timed() {
     long long launches = 0;
     int rc = GSDR_OK;
     while (true) {
-        launch_plain_round(R_, B_, opts.threshold, opts.drop, opts.pigeon, parity, stream,
-                           &launches, e4);
+        launch_step(parity, &launches, e4);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(h_done_, &B_.st->done, sizeof(int32_t), cudaMemcpyDeviceToHost,
@@ -301,7 +314,7 @@ int Job::run() {
     }
     JCUDA(cudaEventRecord(ev_[2], stream));
     // clustering / clusteringDrop (func.cu:1001-1097)
-    init_rounds(R_, B_, stream);
+    init_rounds(R_, B_, batched_ ? 1 : 0, r_max_, stream);
     stats.kernel_launches += 1;
     JCUDA(cudaGetLastError());
     int rc = opts.stage_timing ? loop_timed() : loop_graph();
@@ -310,7 +323,9 @@ int Job::run() {
     JCUDA(cudaMemcpyAsync(h_state_, B_.st, sizeof(RoundState), cudaMemcpyDeviceToHost, stream));
     JCUDA(cudaStreamSynchronize(stream));
     JCUDA(cudaGetLastError());
-    if (h_state_->pair_overflow) return fail(GSDR_EDEVICE, "alignment queue overflow");
+    if (h_state_->error == 2) return fail(GSDR_ENOMEM, "alignment queue overflow");
+    if (h_state_->error) return fail(GSDR_ETIMEOUT, "a device-side wait gave up");
+    if (!batched_ && h_state_->pair_overflow) return fail(GSDR_EDEVICE, "alignment queue overflow");
     float ms = 0;
     cudaEventElapsedTime(&ms, ev_[1], ev_[2]);
     stats.ms_prep = ms;

@@ -19,8 +19,10 @@
 
 namespace gsdr {
 
-constexpr int kMaxK = 8;             // k-mer length handled by the u32 entry format
-constexpr int kMaxPatternWords = 1024;  // 32 lanes x 32 words: 32768 gap-free bases
+constexpr int kMaxPatternWords = 1024;  // 8 warps x 32 lanes x 4 words: 32768 gap-free bases
+constexpr int kAlignClasses = 6;        // pattern length classes of the alignment kernels
+constexpr int kMaxBatch = 1024;         // tentative representatives per batched pass
+constexpr int kTTWords = kMaxBatch / 32;
 
 struct DevReads {
     int32_t n;
@@ -38,27 +40,30 @@ struct DevReads {
     const int64_t* kmer_off;
     int32_t* n_kmer;
     uint32_t* kmer;
-    // pigeon filter (p 1)
-    const int64_t* raw_off;  // the reference's padded byte offsets (copyData)
-    uint16_t* pig;           // 256 inclusive prefix counts per read
-    uint16_t* pig_idx;       // positions, at raw_off[i] + slot
 };
 
 // Per-job round state, in device memory; kernels read their work sizes here so
 // that a whole sequence of rounds can be captured in one CUDA graph.
 struct RoundState {
-    int32_t rep;        // representative of the current round (plain form)
+    int32_t rep;        // plain form: representative of the current round
     int32_t n_remain;   // entries in the current remain list
     int32_t n_next;     // entries written by the compaction
     int32_t next_min;   // smallest still-unclustered index seen by the compaction
-    int32_t n_pairs[2]; // pairs queued for alignment: short / long patterns
+    int32_t n_pairs[kAlignClasses];  // pairs queued per alignment class
     int32_t pair_overflow;
-    int32_t work_filter;
     int32_t done;
     int32_t error;
-    int32_t batch_first;   // batched form: index of the first tentative in `tent`
-    int32_t n_tent;        // batched form: tentatives this pass
-    long long rounds;      // representatives taken so far
+    // batched form
+    int32_t pass;       // pass number (keys of tidx/best carry it), from 1
+    int32_t R;          // tentatives requested for this pass
+    int32_t R_max;
+    int32_t cursor;     // first index not yet considered as a tentative
+    int32_t n_tent;     // tentatives selected this pass
+    int32_t n_acc;      // accepted pairs this pass
+    int32_t acc_overflow;
+    int32_t survivors;  // representatives confirmed this pass
+    int32_t absorbed;   // reads absorbed this pass
+    long long rounds;   // representatives taken so far
     long long passes;
     unsigned long long cnt_prefilter, cnt_word, cnt_aligned, cnt_accepted;
     unsigned long long cells;
@@ -66,35 +71,42 @@ struct RoundState {
 };
 
 struct Pair {
-    int32_t rep;
-    int32_t cand;
+    int32_t rep;   // read index of the representative (or tentative)
+    int32_t cand;  // read index of the candidate
 };
 
 // ---- prep.cu ----
 // Parse + gap-free pack + composition + cutoffs, one warp per read.
 void launch_pack(const DevReads& R, float t, int k, cudaStream_t s);
-// Distinct k-mers with multiplicities for every read (k <= kMaxK).
+// Distinct k-mers with multiplicities for every read (k <= 7).
 int launch_kmers(const DevReads& R, int k, cudaStream_t s);
-// Pigeon index (kernel_createPigeon1/2 semantics).
-void launch_pigeon_index(const DevReads& R, cudaStream_t s);
+int num_sms();
 
 // ---- rounds.cu ----
 struct RoundBuffers {
     RoundState* st;      // device
     int32_t* cluster;    // device, n
     int32_t* remain[2];  // device, n each
-    Pair* pairs;         // device
-    int32_t pair_cap;
-    int32_t* tent;       // batched form: tentative indices
-    uint32_t* accept;    // batched form: accept bits per (tentative, candidate slot)
-    int32_t batch;
+    Pair* pairs;         // device: kAlignClasses segments of seg_cap pairs
+    int32_t seg_cap;
+    // batched form
+    int32_t* tent;       // kMaxBatch tentative read indices (ascending)
+    uint32_t* tidx;      // n: (pass << 12) | tentative index, for reads that are tentatives
+    uint32_t* best;      // n: (pass << 12) | (4095 - i) of the claiming tentative
+    uint32_t* tt;        // kMaxBatch x kTTWords: tentative h accepted tentative i
+    uint32_t* ttrow;     // kTTWords: rows of tt with any bit
+    uint32_t* survive;   // kTTWords
+    Pair* acc;           // accepted pairs of the pass
+    int32_t acc_cap;
 };
-void init_rounds(const DevReads& R, RoundBuffers& B, cudaStream_t s);
-// Launches one plain round (filter, align, compact, advance); `parity` picks
-// which remain buffer is the input.  `count` accumulates kernel launches.
-void launch_plain_round(const DevReads& R, RoundBuffers& B, float t, int drop, int pigeon,
-                        int parity, cudaStream_t s, long long* count, cudaEvent_t* ev4);
-int filter_smem_bytes(int k, int drop);
-int num_sms();
+void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s);
+// One plain round (filter, align, compact, advance); `parity` picks which
+// remain buffer is the input.  `count` accumulates kernel launches; `ev4`
+// (optional) receives events around the filter and alignment stages.
+void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity,
+                        cudaStream_t s, long long* count, cudaEvent_t* ev4);
+// One batched pass (select, filter, align, resolve, compact, advance).
+void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,
+                       long long* count, cudaEvent_t* ev4);
 
 }  // namespace gsdr

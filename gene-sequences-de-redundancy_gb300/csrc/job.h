@@ -36,8 +36,11 @@ private:
     int capture_graph();
     int loop_graph();
     int loop_timed();
+    void launch_step(int parity, long long* count, cudaEvent_t* ev4);
 
     bool own_stream_ = false;
+    bool batched_ = false;
+    int r_max_ = 1;
     int64_t n_bytes_ = 0;
     std::vector<int64_t> pack_off_, kmer_off_;
     void* dmem_ = nullptr;

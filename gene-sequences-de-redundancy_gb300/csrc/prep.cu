@@ -185,7 +185,7 @@ template <int K>
 int kmers_hist_launch(const DevReads& R, cudaStream_t s) {
     constexpr int NB = 1 << (2 * K);
     const int smem = NB * 4 + NB * 2;
-    if (smem > 48 * 1024) {
+    if (smem > 0) {
         cudaError_t e = cudaFuncSetAttribute(k_kmers_hist<K>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return 1;

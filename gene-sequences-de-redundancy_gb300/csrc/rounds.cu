@@ -1,29 +1,43 @@
-// rounds.cu -- the greedy round loop on the device.
+// rounds.cu -- the greedy round loop on the device, plain and batched.
 //
 // Plain form: one representative per round, as the reference's clustering()
 // (cuda-version/func.cu:1001-1066) and clusteringDrop() (func.cu:1068-1097).
-// A round is four kernels that read their sizes from a RoundState in device
-// memory, so rounds run back to back (and inside a CUDA graph) with no host
-// round trip:
-//   k_filter   kernel_preFilter + [kernel_pigeon] + kernel_makeTable/kernel_filter
-//              (func.cu:712-826): warp-ballot over 32 candidates for the
-//              composition bound, then one warp per survivor streams its
-//              (k-mer, count) entries with 16-byte loads against the
-//              representative's table staged in shared memory.  Survivors go
-//              to an alignment queue (two length classes).
-//   k_align_*  kernel_align (func.cu:828-999): warp-per-pair bit-parallel LCS,
-//              marks cluster[j] = representative.
-//   k_compact  updataRemain (func.cu:689-699): drops clustered reads from the
-//              remain list (warp-aggregated atomics) and finds the smallest
-//              unclustered index.
-//   k_advance  updateRepresentative (func.cu:677-687): that index becomes the
-//              next representative.
-// Every decision is a pure function of (representative, candidate), so the
-// order in which candidates are visited does not change any result.
+// A round is a fixed sequence of kernels that read their sizes from a
+// RoundState in device memory, so rounds run back to back (and inside a CUDA
+// graph) with no host round trip:
+//   k_filter      kernel_preFilter + kernel_makeTable/kernel_filter
+//                 (func.cu:712-754, 803-826): one warp per candidate; the
+//                 composition bound first, then the candidate's (k-mer, count)
+//                 entries streamed with 16-byte loads against the
+//                 representative's table staged in shared memory.  Survivors
+//                 are queued for alignment in six length classes.
+//   k_align       kernel_align (func.cu:828-999): bit-parallel LCS on a group
+//                 of G warps with W pattern words per lane (lcs_pipe.cuh).
+//   k_compact     updataRemain (func.cu:689-699): drops clustered reads from
+//                 the remain list and finds the smallest unclustered index.
+//   k_advance     updateRepresentative (func.cu:677-687).
+//
+// Batched form: every decision is a pure function of (representative,
+// candidate), so a pass takes the next R unclustered reads r_1 < ... < r_R as
+// tentative representatives, computes accept(i, j) for every tentative i and
+// every unclustered j > r_i at once, and then replays the reference's order:
+// r_i survives iff no surviving r_h (h < i) accepted it, and each candidate
+// joins the first surviving tentative that accepted it.  That is exactly what
+// R consecutive reference rounds produce.
+//   k_bselect     next R unclustered indices from a forward cursor
+//   k_bfilter     prefilter + word filter of (tentative group, candidate)
+//   k_align       as above, accepted pairs listed instead of applied
+//   k_bsurvive    survival of the tentatives in order (one warp)
+//   k_bclaim      first surviving tentative per candidate (keyed atomicMax)
+//   k_bapply      writes the winners into cluster[]
+//   k_compact, k_badvance
+// R adapts per pass: it halves after a pass in which representatives absorbed
+// many reads (tentatives there mostly repeat each other's work) and doubles
+// otherwise, up to the caller's maximum.  The result does not depend on R.
 #include <cuda_runtime.h>
 
 #include "gsdr_device.cuh"
-#include "lcs.cuh"
+#include "lcs_pipe.cuh"
 
 namespace gsdr {
 
@@ -31,54 +45,43 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kFilterThreads = 256;
-constexpr int kAlignThreads = 128;
-constexpr int kSmallWords = 128;  // pattern words handled by the small-class kernel (W <= 4)
+constexpr int kAlignThreads = 256;  // 8 warps: 8/G groups of G warps
+constexpr int kAbsorbHigh = 64;     // absorbed reads per representative that shrink R
 
 __device__ __forceinline__ bool prefilter_pass(const int4 a, const int4 b, int cut) {
     const int s = min(a.x, b.x) + min(a.y, b.y) + min(a.z, b.z) + min(a.w, b.w);
     return !(s < cut);
 }
 
-// kernel_pigeon (cuda-version/func.cu:756-801), one warp per pair: lane l
-// walks buckets l, l+32, ... with the reference's merge rule.
-__device__ bool pigeon_pass_warp(const DevReads& R, float t, int rep, int q, int lane) {
-    const uint16_t* p1 = R.pig + (size_t)rep * 256;
-    const uint16_t* p2 = R.pig + (size_t)q * 256;
-    const uint16_t* i1 = R.pig_idx + R.raw_off[rep];
-    const uint16_t* i2 = R.pig_idx + R.raw_off[q];
-    const int gap = (int)((float)R.len[rep] - ceilf(__fmul_rn((float)R.len[q], t)));
-    int sum = 0;
-    for (int b = lane; b < 256; b += 32) {
-        int s1 = b > 0 ? p1[b - 1] : 0, e1 = p1[b];
-        int s2 = b > 0 ? p2[b - 1] : 0, e2 = p2[b];
-        while (s1 < e1 && s2 < e2) {
-            const int one = i1[s1], two = i2[s2];
-            if (abs(one - two) >= gap) {
-                s1++;
-                s2++;
-                sum++;
-            } else if (one > two) {
-                s1++;
-            } else {
-                s2++;
-            }
-        }
-    }
-    sum = warp_sum_i(sum);
-    return !(sum < R.cut_pig[q]);
+// Alignment class of a pattern of `words` 32-base words:
+// 0: <=32 (1 warp), 1: <=64 (2 warps), 2: <=128 (4), 3: <=256 (8),
+// 4: <=512 (8 warps, 2 words/lane), 5: <=1024 (8 warps, 4 words/lane).
+__device__ __forceinline__ int align_class(int words) {
+    return words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 256 ? 3
+                                                             : words <= 512 ? 4 : 5;
 }
 
-template <int K, bool DROP, bool PIGEON>
+__device__ __forceinline__ void push_pair(RoundState* st, Pair* pairs, int seg_cap,
+                                          const DevReads& R, int rep, int q) {
+    const int cls = align_class((R.len_gf[q] + 31) >> 5);
+    const int slot = atomicAdd(&st->n_pairs[cls], 1);
+    if (slot < seg_cap) pairs[(size_t)cls * seg_cap + slot] = Pair{rep, q};
+    else st->pair_overflow = 1;
+}
+
+// ---------------------------------------------------------------- plain form
+
+template <int K, bool DROP>
 __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundState* st,
                                                            const int32_t* __restrict__ remain,
-                                                           Pair* pairs, int pair_cap, float t) {
+                                                           Pair* pairs, int seg_cap) {
     extern __shared__ __align__(16) uint16_t table[];
     if (st->done) return;
     const int rep = st->rep;
     const int n = st->n_remain;
     if (n <= 0) return;
-    constexpr int NB = DROP ? 0 : (1 << (2 * K));
     if (!DROP) {
+        constexpr int NB = 1 << (2 * K);
         uint32_t* t32 = reinterpret_cast<uint32_t*>(table);
         for (int i = threadIdx.x; i < NB / 2; i += blockDim.x) t32[i] = 0u;
         __syncthreads();
@@ -93,123 +96,139 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
     }
     const int lane = threadIdx.x & 31;
     const int4 crep = R.comp[rep];
-    const int rep_gf = R.len_gf[rep];
-    unsigned long long n_pf = 0, n_wf = 0, n_al = 0, bytes = 0;
-    while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(&st->work_filter, 32);
-        base = __shfl_sync(kFull, base, 0);
-        if (base >= n) break;
-        const int idx = base + lane;
-        const int j = idx < n ? remain[idx] : -1;
-        bool pass = false;
-        if (j >= 0 && j != rep) {
-            // kernel_preFilter (func.cu:738-754); lossless, so also used in drop mode.
-            pass = prefilter_pass(crep, R.comp[j], R.cut_base[j]);
-            n_pf++;
-        }
-        unsigned m = __ballot_sync(kFull, pass);
-        while (m) {
-            const int src = __ffs(m) - 1;
-            m &= m - 1;
-            const int q = __shfl_sync(kFull, j, src);
-            bool ok = true;
-            if (PIGEON) ok = pigeon_pass_warp(R, t, rep, q, lane);
-            if (!DROP && ok) {
-                // kernel_filter (func.cu:803-826): sum of min(table, count).
-                const int ne = R.n_kmer[q];
-                const int ne4 = (ne + 3) >> 2;
-                const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
-                int sum = 0;
-                for (int i = lane; i < ne4; i += 32) {
-                    const uint4 v = __ldcs(e4 + i);
-                    sum += min((uint32_t)table[v.x >> 16], v.x & 0xffffu);
-                    sum += min((uint32_t)table[v.y >> 16], v.y & 0xffffu);
-                    sum += min((uint32_t)table[v.z >> 16], v.z & 0xffffu);
-                    sum += min((uint32_t)table[v.w >> 16], v.w & 0xffffu);
-                }
-                sum = warp_sum_i(sum);
-                ok = !(sum < R.cut_word[q]);
-                if (lane == 0) {
-                    n_wf++;
-                    bytes += 16ull * ne4;
-                }
+    unsigned n_pf = 0, n_wf = 0, n_al = 0;
+    unsigned long long bytes = 0;
+    const int nwarps = gridDim.x * (kFilterThreads / 32);
+    for (int idx = blockIdx.x * (kFilterThreads / 32) + (threadIdx.x >> 5); idx < n;
+         idx += nwarps) {
+        const int q = remain[idx];
+        if (q == rep) continue;
+        n_pf++;
+        // kernel_preFilter (func.cu:738-754); lossless, so also used in drop mode.
+        if (!prefilter_pass(crep, R.comp[q], R.cut_base[q])) continue;
+        if (!DROP) {
+            // kernel_filter (func.cu:803-826): sum over distinct k-mers of
+            // min(count in representative, count in candidate).
+            n_wf++;
+            const int ne4 = (R.n_kmer[q] + 3) >> 2;
+            const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
+            int sum = 0;
+#pragma unroll 4
+            for (int i = lane; i < ne4; i += 32) {
+                const uint4 v = __ldcs(e4 + i);
+                sum += min((uint32_t)table[v.x >> 16], v.x & 0xffffu);
+                sum += min((uint32_t)table[v.y >> 16], v.y & 0xffffu);
+                sum += min((uint32_t)table[v.z >> 16], v.z & 0xffffu);
+                sum += min((uint32_t)table[v.w >> 16], v.w & 0xffffu);
             }
-            if (ok && lane == 0) {
-                n_al++;
-                const int qgf = R.len_gf[q];
-                const int words = (qgf + 31) >> 5;
-                (void)rep_gf;
-                const int cls = words <= kSmallWords ? 0 : 1;
-                const int half = pair_cap >> 1;
-                const int slot = atomicAdd(&st->n_pairs[cls], 1);
-                if (slot < half) pairs[cls * half + slot] = Pair{rep, q};
-                else st->pair_overflow = 1;
-            }
+            bytes += 16ull * ne4;
+            sum = warp_sum_i(sum);
+            if (sum < R.cut_word[q]) continue;
         }
+        n_al++;
+        if (lane == 0) push_pair(st, pairs, seg_cap, R, rep, q);
     }
-    // per-warp statistics
-    n_pf = __reduce_add_sync(kFull, (unsigned)n_pf);
     if (lane == 0) {
-        atomicAdd(&st->cnt_prefilter, n_pf);
-        if (n_wf) atomicAdd(&st->cnt_word, n_wf);
-        if (n_al) atomicAdd(&st->cnt_aligned, n_al);
-        if (bytes) atomicAdd(&st->filter_bytes, bytes + 0ull);
+        if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
+        if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
+        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
+        if (bytes) atomicAdd(&st->filter_bytes, bytes);
     }
 }
 
-// The pair decision shared by both alignment kernels.
-template <bool SMALL>
-__device__ bool align_pair(const DevReads& R, int rep, int q, int lane) {
-    const int T = R.len_gf[rep];
-    const int qn = R.len_gf[q];
-    const int c = R.cut_base[q];
-    if (T == 0) return false;   // the reference never decides such a pair
-    if (c <= 0) return true;    // LCS >= 0 >= cutoff
-    if (qn < c || T < c) return false;
-    const uint32_t* pq = R.packed + R.pack_off[q];
-    const uint32_t* pt = R.packed + R.pack_off[rep];
-    const int words = (qn + 31) >> 5;
-    if (SMALL) {
-        if (words <= 32) return lcs_reaches_warp<1, true>(pq, qn, pt, T, c, lane);
-        if (words <= 64) return lcs_reaches_warp<2, true>(pq, qn, pt, T, c, lane);
-        return lcs_reaches_warp<4, true>(pq, qn, pt, T, c, lane);
-    } else {
-        if (words <= 256) return lcs_reaches_warp<8, false>(pq, qn, pt, T, c, lane);
-        if (words <= 512) return lcs_reaches_warp<16, false>(pq, qn, pt, T, c, lane);
-        return lcs_reaches_warp<32, false>(pq, qn, pt, T, c, lane);
-    }
+// Decisions that need no alignment; -1 when the LCS must be computed.
+__device__ __forceinline__ int trivial_decision(int T, int q, int c) {
+    if (T == 0) return 0;  // the reference's kernel_align never decides such a pair
+    if (c <= 0) return 1;  // LCS >= 0 >= cutoff
+    if (q < c || T < c) return 0;
+    return -1;
 }
 
-template <bool SMALL>
-__global__ void __launch_bounds__(kAlignThreads) k_align(DevReads R, RoundState* st,
-                                                         const Pair* __restrict__ pairs,
-                                                         int pair_cap, int32_t* cluster,
-                                                         int* work) {
+struct AlignArgs {
+    const Pair* pairs;
+    int seg_cap;
+    int32_t* cluster;
+    int* work;
+    // batched form
+    const uint32_t* tidx;
+    uint32_t* tt;
+    uint32_t* ttrow;
+    Pair* acc;
+    int acc_cap;
+};
+
+template <int G, int W, bool BATCH>
+__global__ void __launch_bounds__(kAlignThreads) k_align(DevReads R, RoundState* st, AlignArgs A,
+                                                         int cls) {
+    constexpr int NG = (kAlignThreads / 32) / G;
+    __shared__ PipeGroup groups[NG];
     if (st->done) return;
-    const int half = pair_cap >> 1;
-    const int np = min(st->n_pairs[SMALL ? 0 : 1], half);
+    if (BATCH && (st->pair_overflow || st->n_tent == 0)) return;
+    const int np = min(st->n_pairs[cls], A.seg_cap);
     if (np <= 0) return;
-    const int lane = threadIdx.x & 31;
-    const Pair* list = pairs + (SMALL ? 0 : half);
+    const int pass = BATCH ? st->pass : 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = warp / G, gw = warp % G;
+    PipeGroup& S = groups[g];
+    const int bar_id = 1 + g, bar_n = G * 32;
+    const Pair* list = A.pairs + (size_t)cls * A.seg_cap;
+    if (gw == 0 && lane == 0) {
+        for (int b = 0; b < 8; b++) {
+            S.ready[b] = 0;
+            S.consumed[b] = 0;
+        }
+        S.stop = 0;
+        S.result = 0;
+        S.error = 0;
+    }
     unsigned long long acc = 0, cells = 0;
     while (true) {
-        int i = 0;
-        if (lane == 0) i = atomicAdd(work, 1);
-        i = __shfl_sync(kFull, i, 0);
+        if (gw == 0 && lane == 0) S.idx = atomicAdd(A.work + cls, 1);
+        group_bar(bar_id, bar_n);
+        const int i = *(volatile int*)&S.idx;
         if (i >= np) break;
         const Pair p = list[i];
-        const bool ok = align_pair<SMALL>(R, p.rep, p.cand, lane);
-        if (lane == 0) {
-            cells += (unsigned long long)R.len_gf[p.rep] * (unsigned long long)R.len_gf[p.cand];
-            if (ok) {
-                cluster[p.cand] = p.rep;
-                acc++;
-            }
+        const int T = R.len_gf[p.rep], q = R.len_gf[p.cand], c = R.cut_base[p.cand];
+        const int trivial = trivial_decision(T, q, c);
+        if (trivial < 0) {
+            const int words = (q + 31) >> 5;
+            const int B = (words + 32 * W - 1) / (32 * W);
+            if (gw < B)
+                lcs_pipe_pair<W>(S, R.packed + R.pack_off[p.cand], q, R.packed + R.pack_off[p.rep],
+                                 T, c, B, gw, lane, &st->error);
         }
+        group_bar(bar_id, bar_n);
+        if (gw == 0 && lane == 0) {
+            const int ok = trivial >= 0 ? trivial : (S.error ? 0 : *(volatile int*)&S.result);
+            cells += (unsigned long long)T * (unsigned long long)q;
+            if (ok) {
+                acc++;
+                if (!BATCH) {
+                    A.cluster[p.cand] = p.rep;
+                } else {
+                    const int slot = atomicAdd(&st->n_acc, 1);
+                    if (slot < A.acc_cap) A.acc[slot] = p;
+                    else st->acc_overflow = 1;
+                    const uint32_t kc = A.tidx[p.cand];
+                    if ((int)(kc >> 12) == pass) {  // a tentative accepted another tentative
+                        const int h = A.tidx[p.rep] & 0xfff, ci = kc & 0xfff;
+                        atomicOr(&A.tt[h * kTTWords + (ci >> 5)], 1u << (ci & 31));
+                        atomicOr(&A.ttrow[h >> 5], 1u << (h & 31));
+                    }
+                }
+            }
+            for (int b = 0; b < 8; b++) {
+                S.ready[b] = 0;
+                S.consumed[b] = 0;
+            }
+            S.stop = 0;
+            S.result = 0;
+            S.error = 0;
+        }
+        group_bar(bar_id, bar_n);
     }
-    if (lane == 0 && (acc || cells)) {
-        atomicAdd(&st->cnt_accepted, acc);
+    if (gw == 0 && lane == 0 && cells) {
+        if (!BATCH) atomicAdd(&st->cnt_accepted, acc);
         atomicAdd(&st->cells, cells);
     }
 }
@@ -243,10 +262,21 @@ __global__ void k_compact(RoundState* st, const int32_t* __restrict__ remain_in,
     if (lane == 0 && local_min != 0x7fffffff) atomicMin(&st->next_min, local_min);
 }
 
+__device__ void reset_align_counters(RoundState* st, int* align_work) {
+    for (int c = 0; c < kAlignClasses; c++) {
+        st->n_pairs[c] = 0;
+        align_work[c] = 0;
+    }
+}
+
 __global__ void k_advance(RoundState* st, int32_t* cluster, int* align_work) {
     if (st->done) return;
     st->rounds += 1;
     st->passes += 1;
+    if (st->error || st->pair_overflow) {
+        st->done = 1;
+        return;
+    }
     const int n = st->n_next;
     if (n == 0) {
         st->done = 1;
@@ -258,108 +288,454 @@ __global__ void k_advance(RoundState* st, int32_t* cluster, int* align_work) {
     st->n_remain = n;
     st->n_next = 0;
     st->next_min = 0x7fffffff;
-    st->n_pairs[0] = 0;
-    st->n_pairs[1] = 0;
-    st->work_filter = 0;
-    align_work[0] = 0;
-    align_work[1] = 0;
+    reset_align_counters(st, align_work);
 }
 
-__global__ void k_init(RoundState* st, int32_t* cluster, int32_t* remain, int n, int* align_work) {
+// ---------------------------------------------------------------- batched form
+
+// Next R unclustered indices at or after the cursor, in increasing order.
+__global__ void __launch_bounds__(1024) k_bselect(RoundState* st, const int32_t* __restrict__ cluster,
+                                                  int n, int32_t* tent, uint32_t* tidx,
+                                                  uint32_t* tt, uint32_t* ttrow, uint32_t* survive,
+                                                  int* align_work) {
+    __shared__ int warp_cnt[32];
+    __shared__ int s_nt;
+    if (st->done) return;
+    const int Rq = st->R;
+    const int pass = st->pass;
+    int pos = st->cursor;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_nt = 0;
+    __syncthreads();
+    while (pos < n) {
+        const int nt = s_nt;
+        if (nt >= Rq) break;
+        const int idx = pos + threadIdx.x;
+        const bool un = idx < n && cluster[idx] == -1;
+        const unsigned m = __ballot_sync(kFull, un);
+        if (lane == 0) warp_cnt[warp] = __popc(m);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < 32; w++) {
+            const int c = warp_cnt[w];
+            if (w < warp) before += c;
+            total += c;
+        }
+        const int rank = nt + before + __popc(m & ((1u << lane) - 1u));
+        if (un && rank < Rq) {
+            tent[rank] = idx;
+            tidx[idx] = ((uint32_t)pass << 12) | (uint32_t)rank;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_nt = min(Rq, nt + total);
+        pos += blockDim.x;
+        __syncthreads();
+    }
+    const int nt = s_nt;
+    for (int i = threadIdx.x; i < nt * kTTWords; i += blockDim.x) tt[i] = 0u;
+    if (threadIdx.x < kTTWords) {
+        ttrow[threadIdx.x] = 0u;
+        survive[threadIdx.x] = 0u;
+    }
+    if (threadIdx.x == 0) {
+        st->n_tent = nt;
+        st->n_acc = 0;
+        st->acc_overflow = 0;
+        st->pair_overflow = 0;
+        st->survivors = 0;
+        st->absorbed = 0;
+        reset_align_counters(st, align_work);
+        if (nt == 0) st->done = 1;
+    }
+}
+
+// Tentatives staged per CTA: RG tables of 4^K u16 in shared memory.
+template <int K>
+struct BatchGroup {
+    static constexpr int RG = K <= 4 ? 32 : K == 5 ? 24 : K == 6 ? 12 : 3;
+    static constexpr int NB = 1 << (2 * K);
+    static constexpr int smem = RG * NB * 2;
+};
+
+template <int K, bool DROP>
+__global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundState* st,
+                                                            const int32_t* __restrict__ remain,
+                                                            const int32_t* __restrict__ tent,
+                                                            Pair* pairs, int seg_cap) {
+    constexpr int RG = DROP ? 32 : BatchGroup<K>::RG;
+    constexpr int NB = BatchGroup<K>::NB;
+    extern __shared__ __align__(16) uint16_t tab[];  // [RG][NB]
+    __shared__ int4 tcomp[32];
+    __shared__ int ttent[32];
+    if (st->done || st->n_tent == 0) return;
+    const int nt = st->n_tent;
+    const int n = st->n_remain;
+    const int ngroups = (nt + RG - 1) / RG;
+    const int parts = max(1, (int)gridDim.x / ngroups);
+    const int lane = threadIdx.x & 31;
+    unsigned n_pf = 0, n_wf = 0, n_al = 0;
+    unsigned long long bytes = 0;
+    int cur_group = -1;
+    for (int item = blockIdx.x; item < ngroups * parts; item += gridDim.x) {
+        const int g = item % ngroups, part = item / ngroups;
+        const int t0 = g * RG;
+        const int ng = min(RG, nt - t0);
+        if (g != cur_group) {
+            __syncthreads();
+            if (threadIdx.x < RG) {
+                const int i = t0 + threadIdx.x;
+                ttent[threadIdx.x] = threadIdx.x < ng ? tent[i] : 0x7fffffff;
+                tcomp[threadIdx.x] = threadIdx.x < ng ? R.comp[tent[i]] : make_int4(0, 0, 0, 0);
+            }
+            if (!DROP) {
+                uint32_t* t32 = reinterpret_cast<uint32_t*>(tab);
+                for (int i = threadIdx.x; i < RG * NB / 2; i += blockDim.x) t32[i] = 0u;
+                __syncthreads();
+                for (int t = 0; t < ng; t++) {
+                    const int rep = ttent[t];
+                    const uint32_t* e = R.kmer + R.kmer_off[rep];
+                    const int ne = R.n_kmer[rep];
+                    for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+                        const uint32_t v = __ldg(e + i);
+                        const uint32_t c = v & 0xffffu;
+                        if (c) tab[t * NB + (v >> 16)] = (uint16_t)c;
+                    }
+                }
+            }
+            __syncthreads();
+            cur_group = g;
+        }
+        // this item's slice of the candidate list, one warp per candidate
+        const int per = (n + parts - 1) / parts;
+        const int lo = part * per, hi = min(n, lo + per);
+        for (int idx = lo + (threadIdx.x >> 5); idx < hi; idx += kFilterThreads / 32) {
+            const int q = remain[idx];
+            // lane t evaluates tentative t: order and composition bound
+            bool ok = false;
+            if (lane < ng) {
+                const int rep = ttent[lane];
+                ok = rep < q && prefilter_pass(tcomp[lane], R.comp[q], R.cut_base[q]);
+            }
+            unsigned mask = __ballot_sync(kFull, ok);
+            n_pf += lane < ng && ttent[lane] < q;
+            if (!mask) continue;
+            if (!DROP) {
+                n_wf += __popc(mask);
+                int sum[RG];
+#pragma unroll
+                for (int t = 0; t < RG; t++) sum[t] = 0;
+                const int ne4 = (R.n_kmer[q] + 3) >> 2;
+                const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
+                for (int i = lane; i < ne4; i += 32) {
+                    const uint4 v = __ldcs(e4 + i);
+                    const uint32_t ev[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const uint32_t km = ev[e] >> 16, c = ev[e] & 0xffffu;
+#pragma unroll
+                        for (int t = 0; t < RG; t++)
+                            if (mask & (1u << t)) sum[t] += min((uint32_t)tab[t * NB + km], c);
+                    }
+                }
+                bytes += 16ull * ne4;
+                const int cw = R.cut_word[q];
+                unsigned pass_mask = 0;
+#pragma unroll
+                for (int t = 0; t < RG; t++) {
+                    if (mask & (1u << t)) {
+                        const int s = warp_sum_i(sum[t]);
+                        if (!(s < cw)) pass_mask |= 1u << t;
+                    }
+                }
+                mask = pass_mask;
+            }
+            if (lane < ng && (mask & (1u << lane))) push_pair(st, pairs, seg_cap, R, ttent[lane], q);
+            n_al += __popc(mask);
+        }
+    }
+    n_pf = warp_sum_i((int)n_pf);
+    if (lane == 0) {
+        if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
+        if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
+        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
+        if (bytes) atomicAdd(&st->filter_bytes, bytes);
+    }
+}
+
+// Survival of the tentatives in greedy order (one warp): a tentative survives
+// iff no surviving earlier tentative accepted it.  Only rows with a bit can
+// claim anything, so only those are visited, in increasing order.
+__global__ void k_bsurvive(RoundState* st, const int32_t* __restrict__ tent,
+                           const uint32_t* __restrict__ tt, const uint32_t* __restrict__ ttrow,
+                           uint32_t* survive, int32_t* cluster) {
+    if (st->done || st->n_tent == 0) return;
+    if (st->pair_overflow || st->acc_overflow) return;
+    const int nt = st->n_tent;
+    const int lane = threadIdx.x;
+    uint32_t claimed = 0;  // bits [32*lane, 32*lane+32) of the claimed set
+    const uint32_t rows = ttrow[lane];
+    for (int w = 0; w < kTTWords; w++) {
+        uint32_t rw = __shfl_sync(kFull, rows, w);
+        while (rw) {
+            const int h = w * 32 + __ffs(rw) - 1;
+            rw &= rw - 1;
+            const uint32_t cw = __shfl_sync(kFull, claimed, h >> 5);
+            if (!((cw >> (h & 31)) & 1u)) claimed |= tt[h * kTTWords + lane];
+        }
+    }
+    uint32_t valid;
+    const int lo = lane * 32;
+    valid = nt >= lo + 32 ? 0xffffffffu : (nt > lo ? ((1u << (nt - lo)) - 1u) : 0u);
+    const uint32_t surv = ~claimed & valid;
+    survive[lane] = surv;
+    uint32_t s = surv;
+    while (s) {
+        const int i = lo + __ffs(s) - 1;
+        s &= s - 1;
+        cluster[tent[i]] = tent[i];
+    }
+    const int count = warp_sum_i(__popc(surv));
+    if (lane == 0) {
+        st->survivors = count;
+        st->rounds += count;
+    }
+}
+
+__global__ void k_bclaim(RoundState* st, const Pair* __restrict__ acc,
+                         const uint32_t* __restrict__ tidx, const uint32_t* __restrict__ survive,
+                         uint32_t* best) {
+    if (st->done || st->n_tent == 0 || st->pair_overflow || st->acc_overflow) return;
+    const int na = st->n_acc;
+    const uint32_t pass = (uint32_t)st->pass;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < na; k += gridDim.x * blockDim.x) {
+        const Pair p = acc[k];
+        const int i = tidx[p.rep] & 0xfff;
+        if ((survive[i >> 5] >> (i & 31)) & 1u) atomicMax(&best[p.cand], (pass << 12) | (4095u - i));
+    }
+}
+
+__global__ void k_bapply(RoundState* st, const Pair* __restrict__ acc,
+                         const uint32_t* __restrict__ tidx, const uint32_t* __restrict__ best,
+                         int32_t* cluster) {
+    if (st->done || st->n_tent == 0 || st->pair_overflow || st->acc_overflow) return;
+    const int na = st->n_acc;
+    const uint32_t pass = (uint32_t)st->pass;
+    unsigned applied = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < na; k += gridDim.x * blockDim.x) {
+        const Pair p = acc[k];
+        const int i = tidx[p.rep] & 0xfff;
+        if (best[p.cand] == ((pass << 12) | (4095u - i))) {
+            cluster[p.cand] = p.rep;
+            applied++;
+        }
+    }
+    applied = __reduce_add_sync(kFull, applied);
+    if ((threadIdx.x & 31) == 0 && applied) {
+        atomicAdd(&st->absorbed, (int)applied);
+        atomicAdd(&st->cnt_accepted, (unsigned long long)applied);
+    }
+}
+
+__global__ void k_badvance(RoundState* st, const int32_t* __restrict__ tent, int* align_work) {
+    if (st->done) return;
+    st->passes += 1;
+    st->pass += 1;
+    if (st->error) {
+        st->done = 1;
+        return;
+    }
+    if (st->pair_overflow || st->acc_overflow) {
+        // queues too small for this many tentatives: the pass changed nothing
+        // (the compaction copied the remain list unchanged); redo it with fewer
+        if (st->R == 1) {
+            st->error = 2;
+            st->done = 1;
+            return;
+        }
+        st->R = max(1, st->R / 8);
+        st->n_next = 0;
+        return;
+    }
+    const int nt = st->n_tent;
+    if (nt > 0) st->cursor = tent[nt - 1] + 1;
+    const int surv = max(1, st->survivors);
+    if (st->absorbed > kAbsorbHigh * surv) st->R = max(1, st->R / 2);
+    else st->R = min(st->R_max, st->R * 2);
+    const int n = st->n_next;
+    st->n_next = 0;
+    st->next_min = 0x7fffffff;
+    if (n == 0) {
+        st->done = 1;
+        return;
+    }
+    st->n_remain = n;
+}
+
+__global__ void k_init(RoundState* st, int32_t* cluster, int32_t* remain, uint32_t* tidx,
+                       uint32_t* best, int n, int batched, int r_max, int* align_work) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        cluster[i] = i == 0 ? 0 : -1;
-        if (i > 0) remain[i - 1] = i;
+        if (batched) {
+            cluster[i] = -1;
+            remain[i] = i;
+            tidx[i] = 0xffffffffu;
+            best[i] = 0u;
+        } else {
+            cluster[i] = i == 0 ? 0 : -1;
+            if (i > 0) remain[i - 1] = i;
+        }
     }
     if (i == 0) {
         RoundState s = {};
         s.rep = 0;
-        s.n_remain = n - 1;
+        s.n_remain = batched ? n : n - 1;
         s.next_min = 0x7fffffff;
         s.done = n <= 0 ? 1 : 0;
+        s.pass = 1;
+        s.R = 1;
+        s.R_max = r_max;
         *st = s;
-        align_work[0] = 0;
-        align_work[1] = 0;
+        for (int c = 0; c < kAlignClasses; c++) align_work[c] = 0;
     }
 }
 
-template <int K, bool DROP, bool PIGEON>
-void launch_filter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, float t,
-                     cudaStream_t s) {
+// ---------------------------------------------------------------- launchers
+
+template <class KernelT>
+int grid_for(KernelT kernel, int threads, int smem, int cap_per_sm) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > cap_per_sm) per_sm = cap_per_sm;
+    return num_sms() * per_sm;
+}
+
+template <int K, bool DROP>
+void launch_filter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, cudaStream_t s) {
     const int smem = DROP ? 0 : (1 << (2 * K)) * 2;
     static int grid = 0;
     if (!grid) {
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(k_filter<K, DROP, PIGEON>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_filter<K, DROP, PIGEON>,
-                                                      kFilterThreads, smem);
-        if (per_sm < 1) per_sm = 1;
-        if (per_sm > 4) per_sm = 4;
-        grid = num_sms() * per_sm;
+        if (smem > 0)
+            cudaFuncSetAttribute(k_filter<K, DROP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+        grid = grid_for(k_filter<K, DROP>, kFilterThreads, smem, 8);
     }
-    k_filter<K, DROP, PIGEON><<<grid, kFilterThreads, smem, s>>>(R, B.st, remain, B.pairs,
-                                                                 B.pair_cap, t);
+    k_filter<K, DROP><<<grid, kFilterThreads, smem, s>>>(R, B.st, remain, B.pairs, B.seg_cap);
 }
 
-template <bool DROP, bool PIGEON>
-void launch_filter_k(const DevReads& R, RoundBuffers& B, const int32_t* remain, float t, int k,
-                     cudaStream_t s) {
-    switch (k) {
-        case 4: launch_filter_t<4, DROP, PIGEON>(R, B, remain, t, s); break;
-        case 5: launch_filter_t<5, DROP, PIGEON>(R, B, remain, t, s); break;
-        case 6: launch_filter_t<6, DROP, PIGEON>(R, B, remain, t, s); break;
-        default: launch_filter_t<7, DROP, PIGEON>(R, B, remain, t, s); break;
+template <int K, bool DROP>
+void launch_bfilter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, cudaStream_t s) {
+    const int smem = DROP ? 0 : BatchGroup<K>::smem;
+    static int grid = 0;
+    if (!grid) {
+        if (smem > 0)
+            cudaFuncSetAttribute(k_bfilter<K, DROP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+        grid = grid_for(k_bfilter<K, DROP>, kFilterThreads, smem, 8);
     }
+    k_bfilter<K, DROP><<<grid, kFilterThreads, smem, s>>>(R, B.st, remain, B.tent, B.pairs,
+                                                          B.seg_cap);
+}
+
+template <bool BATCH>
+void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain, int drop,
+                       cudaStream_t s) {
+    if (drop) {
+        if (BATCH) launch_bfilter_t<4, true>(R, B, remain, s);
+        else launch_filter_t<4, true>(R, B, remain, s);
+        return;
+    }
+    switch (R.k) {
+        case 4:
+            BATCH ? launch_bfilter_t<4, false>(R, B, remain, s) : launch_filter_t<4, false>(R, B, remain, s);
+            break;
+        case 5:
+            BATCH ? launch_bfilter_t<5, false>(R, B, remain, s) : launch_filter_t<5, false>(R, B, remain, s);
+            break;
+        case 6:
+            BATCH ? launch_bfilter_t<6, false>(R, B, remain, s) : launch_filter_t<6, false>(R, B, remain, s);
+            break;
+        default:
+            BATCH ? launch_bfilter_t<7, false>(R, B, remain, s) : launch_filter_t<7, false>(R, B, remain, s);
+            break;
+    }
+}
+
+template <int G, int W, bool BATCH>
+void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
+    static int grid = 0;
+    if (!grid) grid = grid_for(k_align<G, W, BATCH>, kAlignThreads, 0, 8);
+    AlignArgs A;
+    A.pairs = B.pairs;
+    A.seg_cap = B.seg_cap;
+    A.cluster = B.cluster;
+    A.work = reinterpret_cast<int*>(B.st + 1);
+    A.tidx = B.tidx;
+    A.tt = B.tt;
+    A.ttrow = B.ttrow;
+    A.acc = B.acc;
+    A.acc_cap = B.acc_cap;
+    k_align<G, W, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, A, cls);
+}
+
+template <bool BATCH>
+void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s) {
+    launch_align_t<1, 1, BATCH>(R, B, 0, s);
+    launch_align_t<2, 1, BATCH>(R, B, 1, s);
+    launch_align_t<4, 1, BATCH>(R, B, 2, s);
+    launch_align_t<8, 1, BATCH>(R, B, 3, s);
+    launch_align_t<8, 2, BATCH>(R, B, 4, s);
+    launch_align_t<8, 4, BATCH>(R, B, 5, s);
 }
 
 }  // namespace
 
-int filter_smem_bytes(int k, int drop) { return drop ? 0 : (1 << (2 * k)) * 2; }
-
-// Device work counters for the two alignment kernels live right after the
-// RoundState in the same allocation.
+// Work counters of the alignment classes live right after the RoundState in
+// the same allocation.
 static int* align_work_of(RoundState* st) { return reinterpret_cast<int*>(st + 1); }
 
-void init_rounds(const DevReads& R, RoundBuffers& B, cudaStream_t s) {
+void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s) {
     const int n = R.n;
     const int threads = 256;
     const int blocks = n > 0 ? (n + threads - 1) / threads : 1;
-    k_init<<<blocks, threads, 0, s>>>(B.st, B.cluster, B.remain[0], n, align_work_of(B.st));
+    k_init<<<blocks, threads, 0, s>>>(B.st, B.cluster, B.remain[0], B.tidx, B.best, n, batched,
+                                      r_max, align_work_of(B.st));
 }
 
-void launch_plain_round(const DevReads& R, RoundBuffers& B, float t, int drop, int pigeon,
-                        int parity, cudaStream_t s, long long* count, cudaEvent_t* ev4) {
+void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,
+                        long long* count, cudaEvent_t* ev4) {
     const int32_t* rin = B.remain[parity];
     int32_t* rout = B.remain[parity ^ 1];
     if (ev4) cudaEventRecord(ev4[0], s);
-    if (drop) {
-        launch_filter_k<true, false>(R, B, rin, t, R.k, s);
-    } else if (pigeon) {
-        launch_filter_k<false, true>(R, B, rin, t, R.k, s);
-    } else {
-        launch_filter_k<false, false>(R, B, rin, t, R.k, s);
-    }
+    launch_filter_any<false>(R, B, rin, drop, s);
     if (ev4) cudaEventRecord(ev4[1], s);
-    static int grid_small = 0, grid_large = 0;
-    if (!grid_small) {
-        int a = 0, b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_align<true>, kAlignThreads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_align<false>, kAlignThreads, 0);
-        grid_small = num_sms() * (a > 0 ? a : 1);
-        grid_large = num_sms() * (b > 0 ? b : 1);
-    }
-    int* aw = align_work_of(B.st);
-    k_align<true><<<grid_small, kAlignThreads, 0, s>>>(R, B.st, B.pairs, B.pair_cap, B.cluster,
-                                                       aw + 0);
-    k_align<false><<<grid_large, kAlignThreads, 0, s>>>(R, B.st, B.pairs, B.pair_cap, B.cluster,
-                                                        aw + 1);
+    launch_align_classes<false>(R, B, s);
     if (ev4) cudaEventRecord(ev4[2], s);
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
-    k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, aw);
+    k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 5;
+    if (count) *count += 3 + kAlignClasses;
+}
+
+void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,
+                       long long* count, cudaEvent_t* ev4) {
+    const int32_t* rin = B.remain[parity];
+    int32_t* rout = B.remain[parity ^ 1];
+    k_bselect<<<1, 1024, 0, s>>>(B.st, B.cluster, R.n, B.tent, B.tidx, B.tt, B.ttrow, B.survive,
+                                 align_work_of(B.st));
+    if (ev4) cudaEventRecord(ev4[0], s);
+    launch_filter_any<true>(R, B, rin, drop, s);
+    if (ev4) cudaEventRecord(ev4[1], s);
+    launch_align_classes<true>(R, B, s);
+    if (ev4) cudaEventRecord(ev4[2], s);
+    k_bsurvive<<<1, 32, 0, s>>>(B.st, B.tent, B.tt, B.ttrow, B.survive, B.cluster);
+    const int g = num_sms() * 2;
+    k_bclaim<<<g, 256, 0, s>>>(B.st, B.acc, B.tidx, B.survive, B.best);
+    k_bapply<<<g, 256, 0, s>>>(B.st, B.acc, B.tidx, B.best, B.cluster);
+    k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
+    k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st));
+    if (ev4) cudaEventRecord(ev4[3], s);
+    if (count) *count += 7 + kAlignClasses;
 }
 
 }  // namespace gsdr

@@ -100,11 +100,11 @@ def test_c3_recipe_slice_drop(tmp_path):
 def _mixed_edge_fasta(seed=9):
     rng = np.random.default_rng(seed)
     recs = []
-    base = rng.choice(list(b"ACGT"), 700).tobytes()
+    base = np.frombuffer(b"ACGT", dtype=np.uint8)[rng.integers(0, 4, 700)].tobytes()
     for i in range(60):
         s = bytearray(base[: rng.integers(150, 700)])
         for _ in range(rng.integers(0, 12)):
-            s[rng.integers(0, len(s))] = rng.choice(list(b"ACGTNRYacgtnu"))
+            s[rng.integers(0, len(s))] = int(rng.choice(list(b"ACGTNRYacgtnu")))
         if i % 7 == 0:
             s += b"\r"
         recs.append(b">r%d desc\n" % i + bytes(s) + b"\n")
