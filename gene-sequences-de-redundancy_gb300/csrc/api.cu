@@ -172,6 +172,10 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     stats.drop = opts.drop;
     stats.pigeon = opts.pigeon;
     batched_ = opts.batch != 1;
+    {
+        const char* tr = std::getenv("GSDR_TRACE");
+        trace_ = tr && tr[0] == '1';
+    }
     r_max_ = opts.batch == 0 ? 256 : (opts.batch > kMaxBatch ? kMaxBatch : opts.batch);
     stats.batch = batched_ ? r_max_ : 1;
     Plan P;
@@ -283,6 +287,16 @@ int Job::loop_timed() {
         cudaEventElapsedTime(&b, e4[1], e4[2]);
         fms += a;
         ams += b;
+        if (trace_) {
+            // per-step trace on stderr: the state after the step
+            RoundState h;
+            if (cudaMemcpy(&h, B_.st, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess)
+                std::fprintf(stderr,
+                             "gsdr trace: step %lld rounds %lld tentatives %d R %d remain %d "
+                             "aligned %llu filter %.3f ms align %.3f ms\n",
+                             (long long)h.passes, (long long)h.rounds, h.n_tent, h.R, h.n_remain,
+                             (unsigned long long)h.cnt_aligned, a, b);
+        }
         parity ^= 1;
         if (*h_done_) break;
     }

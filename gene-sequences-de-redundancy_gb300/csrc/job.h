@@ -40,6 +40,7 @@ private:
 
     bool own_stream_ = false;
     bool batched_ = false;
+    bool trace_ = false;  // GSDR_TRACE=1: per-step stage times on stderr (timed mode)
     int r_max_ = 1;
     int64_t n_bytes_ = 0;
     std::vector<int64_t> pack_off_, kmer_off_;

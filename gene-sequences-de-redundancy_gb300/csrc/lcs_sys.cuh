@@ -1,0 +1,315 @@
+// lcs_sys.cuh -- systolic bit-parallel LCS decision on a group of warps.
+//
+// Decides LCS(pattern, text) >= c, the test of the reference's kernel_align
+// (cuda-version/func.cu:828-999, a full O(q*T) DP per thread), with Hyyro's
+// recurrence over pattern bits:
+//     U = V & M[x];  V' = (V + U) | (V & ~M[x]);   LCS = zeros of V.
+// Pattern = candidate, text = representative.  Lane l of warp b holds the W
+// pattern words (b*32 + l)*W .. +W-1.  The warp is a systolic array: at local
+// step s lane l applies text base x = s - l, taking the carry of the addition
+// from lane l-1's step s-1 (one shuffle per step), so a step is one short
+// dependent chain instead of a warp-wide carry resolution.  Between warps the
+// top lane's carry-out sequence (one bit per text base) is the next warp's
+// lane-0 carry-in sequence, handed over in 32-bit words through a ring in
+// shared memory.  Text bases come from a per-warp 64-entry ring (written twice
+// so that a lane-skewed window is contiguous), one 32-bit word per base whose
+// bytes hold the sign-coded high bit, low bit and "no base" flag; prmt turns
+// each byte into a full mask.
+//
+// Bases outside the text ("no base": pipeline fill before base 0, drain after
+// base T-1) must leave V unchanged.  The flag only clears U: with U = 0 and a
+// zero carry-in, V + U + 0 = V and V' = V | (V & ~M) = V for any M; the carry
+// out is then zero too, so by induction every carry-in of such a step is zero.
+//
+// Decisions, taken every kSysCk blocks of 32 bases by the group's last warp
+// from the zero counts every warp publishes:
+//   accept  LCS(pattern, text[0..X]) >= c (never decreases with X);
+//   reject  Z(q-R) + min(R, q) < c, R = bases after X, Z(i) = zeros below
+//           pattern position i: any common subsequence has <= Z(i) matches
+//           with text[0..X] and <= min(q-i, R) after, maximal at i = q-R.
+// Every wait is bounded (kSpinLimit polls) and reports an error instead of
+// hanging.
+#pragma once
+#include <stdint.h>
+
+#include "lcs.cuh"
+
+namespace gsdr {
+
+constexpr int kSysRing = 4;     // carry words in flight between two warps
+constexpr int kSysZRing = 16;   // checkpoints kept per warp
+constexpr int kSysCk = 4;       // blocks of 32 bases between checkpoints
+constexpr int kSpinLimit = 1 << 22;
+
+struct SysGroup {
+    uint32_t carries[8][kSysRing];
+    int zc[8][kSysZRing];    // zeros of the warp's words at a checkpoint
+    int zp[8][kSysZRing];    // zeros below q - R at that checkpoint
+    int zf[8];               // zeros at the end of the text
+    int ready[8];            // carry words published by warp b
+    int consumed[8];         // carry words of warp b read by warp b+1
+    uint32_t ring[8][128];   // text bases, sign-coded bytes
+    int stop;
+    int result;
+    int idx;
+    int error;
+};
+
+__device__ __forceinline__ int vload(const int* p) { return *(volatile const int*)p; }
+__device__ __forceinline__ void vstore(int* p, int v) { *(volatile int*)p = v; }
+
+__device__ __forceinline__ void group_bar(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+__device__ __forceinline__ bool spin_until_ge(const int* p, int target, const int* stop) {
+    for (int it = 0; it < kSpinLimit; it++) {
+        if (vload(p) >= target) return true;
+        if (vload(stop)) return true;
+        if (it > 64) __nanosleep(20);
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t valid_bits(int q, int w) {
+    const int rem = q - 32 * w;
+    return rem >= 32 ? 0xffffffffu : (rem > 0 ? ((1u << rem) - 1u) : 0u);
+}
+
+template <int W>
+__device__ __forceinline__ int zeros_below(const uint32_t (&V)[W], int w0, int lim) {
+    int z = 0;
+#pragma unroll
+    for (int i = 0; i < W; i++) z += __popc(~V[i] & valid_bits(lim, w0 + i));
+    return z;
+}
+
+// Replicates the sign bit of byte `SEL` of x into all 32 bits.
+template <int SEL>
+__device__ __forceinline__ uint32_t sign_mask(uint32_t x) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "n"(0x8888 | (SEL * 0x1111)));
+    return r;
+}
+
+// Sign-coded text base: byte 0 = high bit, byte 1 = low bit, byte 2 = no base.
+__device__ __forceinline__ uint32_t base_word(uint32_t code, bool valid) {
+    if (!valid) return 0x00800000u;
+    return ((code & 2u) ? 0x80u : 0u) | ((code & 1u) ? 0x8000u : 0u);
+}
+
+__device__ __forceinline__ void sys_fail(SysGroup& S, int* err_flag, int lane) {
+    if (lane == 0) {
+        atomicExch(err_flag, 1);
+        vstore(&S.error, 1);
+        vstore(&S.stop, 1);
+    }
+}
+
+// Eight steps of the systolic array from ring slot rb[0..7].
+//   MULTI: lane 0 takes its carry-in from cin8 (the previous warp's carries,
+//          bit j for step j) and lane 31 collects its carry-outs into out8;
+//          otherwise lane 0's carry-in is zero.
+//   SNAP:  lane l copies V into snapV after the step j == tj (per lane).
+template <int W, bool MULTI, bool SNAP>
+__device__ __forceinline__ void sys_steps8(const uint32_t* __restrict__ rb,
+                                           const uint32_t (&H)[W], const uint32_t (&Lo)[W],
+                                           uint32_t (&V)[W], uint32_t (&snapV)[W],
+                                           uint32_t& from, uint32_t cin8, uint32_t& out8,
+                                           uint32_t not_lane0, int tj, int jbase, int lane) {
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        uint32_t cin = from;
+        if (MULTI) cin = not_lane0 ? from : ((cin8 >> j) & 1u);
+        const uint32_t b = rb[j];
+        const uint32_t ch = sign_mask<0>(b), cl = sign_mask<1>(b), inv = sign_mask<2>(b);
+#pragma unroll
+        for (int i = 0; i < W; i++) {
+            const uint32_t m = ~((H[i] ^ ch) | (Lo[i] ^ cl));
+            const uint32_t u = V[i] & m & ~inv;
+            const uint64_t t = (uint64_t)V[i] + u + cin;
+            cin = (uint32_t)(t >> 32);
+            V[i] = (uint32_t)t | (V[i] & ~m);
+        }
+        if (MULTI) out8 |= cin << j;
+        // lane 0 receives its own carry-out from the shuffle: a single warp
+        // clears it (its lane-0 carry-in is zero); a group member ignores it
+        from = __shfl_up_sync(0xffffffffu, cin, 1);
+        if (!MULTI) from &= not_lane0;
+        if (SNAP && jbase + j == tj) {
+#pragma unroll
+            for (int i = 0; i < W; i++) snapV[i] = V[i];
+        }
+    }
+}
+
+// One block of 32 steps (four unrolled groups of eight).
+template <int W, bool MULTI, bool SNAP>
+__device__ __forceinline__ void sys_block(const uint32_t* __restrict__ rb, const uint32_t (&H)[W],
+                                          const uint32_t (&Lo)[W], uint32_t (&V)[W],
+                                          uint32_t (&snapV)[W], uint32_t& from, uint32_t cin_word,
+                                          uint32_t& cout_word, uint32_t not_lane0, int tj,
+                                          int lane) {
+    cout_word = 0;
+#pragma unroll 1
+    for (int g = 0; g < 4; g++) {
+        uint32_t out8 = 0;
+        sys_steps8<W, MULTI, SNAP>(rb + 8 * g, H, Lo, V, snapV, from, cin_word >> (8 * g), out8,
+                                   not_lane0, tj, 8 * g, lane);
+        if (MULTI) cout_word |= out8 << (8 * g);
+    }
+}
+
+// The decision of one pair on B warps of a group (gw = this warp's index).
+// The result lands in S.result (1 accept, 0 reject) once the group meets at
+// its barrier; S.error is set if a wait gave up.
+template <int W>
+__device__ void lcs_sys_pair(SysGroup& S, const uint32_t* __restrict__ pq, int q,
+                             const uint32_t* __restrict__ pt, int T, int c, int B, int gw,
+                             int lane, int* err_flag) {
+    const int w0 = (gw * 32 + lane) * W;
+    uint32_t H[W], Lo[W], V[W], snapV[W];
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        const int w = w0 + i;
+        uint32_t hi = 0, lo = 0;
+        if (w * 32 < q) planes32(__ldg(pq + 2 * w), __ldg(pq + 2 * w + 1), hi, lo);
+        H[i] = hi;
+        Lo[i] = lo;
+        V[i] = 0xffffffffu;
+        snapV[i] = 0xffffffffu;
+    }
+    uint32_t* ring = S.ring[gw];
+#pragma unroll
+    for (int r = 0; r < 4; r++) ring[lane + 32 * r] = base_word(0, false);
+    __syncwarp();
+    const int M = (T + 31 + 31) >> 5;  // blocks of 32 steps: steps 0 .. T+30
+    const bool multi = B > 1;
+    const bool producer = gw < B - 1;
+    const uint32_t not_lane0 = lane == 0 ? 0u : 0xffffffffu;
+    uint32_t from = 0;   // carry from lane l-1 at the previous step
+    uint32_t wprev = 0;  // top lane: carry bits of the word being completed
+    bool decided = false;
+    for (int m = 0; m < M; m++) {
+        if (vload(&S.stop)) return;
+        uint32_t cin_word = 0;
+        if (gw > 0) {
+            if (!spin_until_ge(&S.ready[gw - 1], m + 1, &S.stop)) {
+                sys_fail(S, err_flag, lane);
+                return;
+            }
+            if (vload(&S.stop)) return;
+            __threadfence_block();
+            cin_word = *(volatile uint32_t*)&S.carries[gw - 1][m % kSysRing];
+            __syncwarp();
+            if (lane == 0) vstore(&S.consumed[gw - 1], m + 1);
+        }
+        // this block's text bases 32m .. 32m+31 into the ring (twice)
+        {
+            const int x = 32 * m + lane;
+            uint32_t code = 0;
+            if (x < T) code = (__ldg(pt + (x >> 4)) >> (30 - 2 * (x & 15))) & 3u;
+            const uint32_t bw = base_word(code, x < T);
+            ring[x & 63] = bw;
+            ring[(x & 63) + 64] = bw;
+        }
+        __syncwarp();
+        const uint32_t* rb = ring + ((32 * m - lane) & 63);
+        // Zero-count snapshots for the checkpoint at base 32m'-1 (m' = next
+        // phase-0 block): lane 0 reaches it at step 31 of the phase kSysCk-1
+        // block, lane l >= 1 at step l-1 of the phase-0 block.
+        const int phase = m % kSysCk;
+        uint32_t cout_word = 0;
+        if (phase == kSysCk - 1 || (phase == 0 && m > 0)) {
+            const int tj = phase == 0 ? (lane == 0 ? -1 : lane - 1) : (lane == 0 ? 31 : -1);
+            if (multi)
+                sys_block<W, true, true>(rb, H, Lo, V, snapV, from, cin_word, cout_word, not_lane0,
+                                         tj, lane);
+            else
+                sys_block<W, false, true>(rb, H, Lo, V, snapV, from, cin_word, cout_word,
+                                          not_lane0, tj, lane);
+        } else {
+            if (multi)
+                sys_block<W, true, false>(rb, H, Lo, V, snapV, from, cin_word, cout_word,
+                                          not_lane0, -1, lane);
+            else
+                sys_block<W, false, false>(rb, H, Lo, V, snapV, from, cin_word, cout_word,
+                                           not_lane0, -1, lane);
+        }
+        __syncwarp();
+        const bool last_block = m == M - 1;
+        // end of text: final zero counts, published before the last carry word
+        if (last_block) {
+            const int zf = warp_sum_i(zeros_below<W>(V, w0, q));
+            if (lane == 0) S.zf[gw] = zf;
+        }
+        // top lane's carry-outs this block: bits for bases 32m-31 .. 32m
+        // (step j carries base 32m+j-31): bits 1..31 finish word m-1, bit 31 of
+        // the block is bit 0 of word m.
+        if (producer) {
+            const uint32_t cw = __shfl_sync(0xffffffffu, cout_word, 31);
+            const uint32_t wdone = wprev | (cw << 1);
+            const uint32_t wlast = cw >> 31;
+            const int nw = last_block ? 2 : 1;  // words m-1 (and m at the end)
+            for (int k2 = 0; k2 < nw; k2++) {
+                const int widx = m - 1 + k2;
+                if (widx < 0) continue;
+                if (!spin_until_ge(&S.consumed[gw], widx + 1 - kSysRing, &S.stop)) {
+                    sys_fail(S, err_flag, lane);
+                    return;
+                }
+                if (lane == 0) S.carries[gw][widx % kSysRing] = k2 == 0 ? wdone : wlast;
+                __threadfence_block();
+                __syncwarp();
+                if (lane == 0) vstore(&S.ready[gw], widx + 1);
+            }
+            wprev = wlast;
+        }
+        // checkpoint for base 32m-1, decided by the last warp
+        const int Xck = 32 * m - 1;
+        if (phase == 0 && m > 0 && Xck < T - 1) {
+            const int Rck = T - 1 - Xck;
+            const int lim = q - Rck;
+            const int zf_ck = warp_sum_i(zeros_below<W>(snapV, w0, q));
+            const int zp_ck = lim > 0 ? warp_sum_i(zeros_below<W>(snapV, w0, lim)) : 0;
+            const int slot = (m / kSysCk) % kSysZRing;
+            if (lane == 0) {
+                S.zc[gw][slot] = zf_ck;
+                S.zp[gw][slot] = zp_ck;
+            }
+            __threadfence_block();
+            __syncwarp();
+            if (gw == B - 1) {
+                int zt = 0, zpt = 0;
+                for (int b2 = 0; b2 < B; b2++) {
+                    zt += *(volatile int*)&S.zc[b2][slot];
+                    zpt += *(volatile int*)&S.zp[b2][slot];
+                }
+                const int ub = (lim > 0 ? zpt : 0) + min(Rck, q);
+                int d = -1;
+                if (zt >= c) d = 1;
+                else if (ub < c) d = 0;
+                if (d >= 0) {
+                    if (lane == 0) {
+                        vstore(&S.result, d);
+                        __threadfence_block();
+                        vstore(&S.stop, 1);
+                    }
+                    decided = true;
+                }
+            }
+        }
+        if (decided) return;
+    }
+    if (gw == B - 1) {
+        int zt = 0;
+        for (int b2 = 0; b2 < B; b2++) zt += *(volatile int*)&S.zf[b2];
+        if (lane == 0) {
+            vstore(&S.result, zt >= c ? 1 : 0);
+            __threadfence_block();
+            vstore(&S.stop, 1);
+        }
+    }
+}
+
+}  // namespace gsdr

@@ -12,7 +12,7 @@
 //                 representative's table staged in shared memory.  Survivors
 //                 are queued for alignment in six length classes.
 //   k_align       kernel_align (func.cu:828-999): bit-parallel LCS on a group
-//                 of G warps with W pattern words per lane (lcs_pipe.cuh).
+//                 of G warps with W pattern words per lane (lcs_sys.cuh).
 //   k_compact     updataRemain (func.cu:689-699): drops clustered reads from
 //                 the remain list and finds the smallest unclustered index.
 //   k_advance     updateRepresentative (func.cu:677-687).
@@ -37,7 +37,7 @@
 #include <cuda_runtime.h>
 
 #include "gsdr_device.cuh"
-#include "lcs_pipe.cuh"
+#include "lcs_sys.cuh"
 
 namespace gsdr {
 
@@ -53,9 +53,9 @@ __device__ __forceinline__ bool prefilter_pass(const int4 a, const int4 b, int c
     return !(s < cut);
 }
 
-// Alignment class of a pattern of `words` 32-base words:
-// 0: <=32 (1 warp), 1: <=64 (2 warps), 2: <=128 (4), 3: <=256 (8),
-// 4: <=512 (8 warps, 2 words/lane), 5: <=1024 (8 warps, 4 words/lane).
+// Alignment class of a pattern of `words` 32-base words (warps x words/lane):
+// 0: <=32 (1x1), 1: <=64 (1x2), 2: <=128 (2x2), 3: <=256 (4x2), 4: <=512 (8x2),
+// 5: <=1024 (8x4).
 __device__ __forceinline__ int align_class(int words) {
     return words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 256 ? 3
                                                              : words <= 512 ? 4 : 5;
@@ -158,10 +158,10 @@ struct AlignArgs {
 };
 
 template <int G, int W, bool BATCH>
-__global__ void __launch_bounds__(kAlignThreads) k_align(DevReads R, RoundState* st, AlignArgs A,
+__global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundState* st, AlignArgs A,
                                                          int cls) {
     constexpr int NG = (kAlignThreads / 32) / G;
-    __shared__ PipeGroup groups[NG];
+    __shared__ SysGroup groups[NG];
     if (st->done) return;
     if (BATCH && (st->pair_overflow || st->n_tent == 0)) return;
     const int np = min(st->n_pairs[cls], A.seg_cap);
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kAlignThreads) k_align(DevReads R, RoundState*
     const int pass = BATCH ? st->pass : 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = warp / G, gw = warp % G;
-    PipeGroup& S = groups[g];
+    SysGroup& S = groups[g];
     const int bar_id = 1 + g, bar_n = G * 32;
     const Pair* list = A.pairs + (size_t)cls * A.seg_cap;
     if (gw == 0 && lane == 0) {
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kAlignThreads) k_align(DevReads R, RoundState*
             const int words = (q + 31) >> 5;
             const int B = (words + 32 * W - 1) / (32 * W);
             if (gw < B)
-                lcs_pipe_pair<W>(S, R.packed + R.pack_off[p.cand], q, R.packed + R.pack_off[p.rep],
+                lcs_sys_pair<W>(S, R.packed + R.pack_off[p.cand], q, R.packed + R.pack_off[p.rep],
                                  T, c, B, gw, lane, &st->error);
         }
         group_bar(bar_id, bar_n);
@@ -681,9 +681,9 @@ void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s)
 template <bool BATCH>
 void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s) {
     launch_align_t<1, 1, BATCH>(R, B, 0, s);
-    launch_align_t<2, 1, BATCH>(R, B, 1, s);
-    launch_align_t<4, 1, BATCH>(R, B, 2, s);
-    launch_align_t<8, 1, BATCH>(R, B, 3, s);
+    launch_align_t<1, 2, BATCH>(R, B, 1, s);
+    launch_align_t<2, 2, BATCH>(R, B, 2, s);
+    launch_align_t<4, 2, BATCH>(R, B, 3, s);
     launch_align_t<8, 2, BATCH>(R, B, 4, s);
     launch_align_t<8, 4, BATCH>(R, B, 5, s);
 }
