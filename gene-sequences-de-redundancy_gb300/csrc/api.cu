@@ -105,6 +105,7 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     R.kmer_off = c.take<int64_t>(n + 1);
     R.n_kmer = c.take<int32_t>(n);
     R.kmer = c.take<uint32_t>((size_t)P.kmer_off[n] + 8);
+    R.bm = c.take<uint32_t>(2 * (size_t)P.pack_off[n] + 8);
     B.st = reinterpret_cast<RoundState*>(c.take<char>(sizeof(RoundState) + 4 * 64));
     B.cluster = c.take<int32_t>(n);
     B.remain[0] = c.take<int32_t>(n);
@@ -318,7 +319,8 @@ int Job::run() {
     // baseToNumber + compressData + createCutoff + createPrefix (func.cu:139-403)
     JCUDA(cudaMemsetAsync(R_.packed, 0, sizeof(uint32_t) * ((size_t)pack_off_[n] + 8), stream));
     launch_pack(R_, opts.threshold, k, stream);
-    stats.kernel_launches += 1;
+    launch_planes(R_, stream);
+    stats.kernel_launches += 2;
     JCUDA(cudaGetLastError());
     // createWords + sortWords + mergeWords (func.cu:405-653)
     if (!drop) {

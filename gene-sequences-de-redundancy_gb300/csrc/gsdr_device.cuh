@@ -40,6 +40,10 @@ struct DevReads {
     const int64_t* kmer_off;
     int32_t* n_kmer;
     uint32_t* kmer;
+    // base bit-planes of the gap-free read: plane c (0..3) of read i starts
+    // at bm[2*pack_off[i] + c*(pack_off[i+1]-pack_off[i])/2]; bit b of word w
+    // is set iff base 32w+b equals c (bits past the read are zero)
+    uint32_t* bm;
 };
 
 // Per-job round state, in device memory; kernels read their work sizes here so
@@ -80,6 +84,8 @@ struct Pair {
 void launch_pack(const DevReads& R, float t, int k, cudaStream_t s);
 // Distinct k-mers with multiplicities for every read (k <= 7).
 int launch_kmers(const DevReads& R, int k, cudaStream_t s);
+// Base bit-planes of every read (after launch_pack).
+void launch_planes(const DevReads& R, cudaStream_t s);
 int num_sms();
 
 // ---- rounds.cu ----

@@ -212,6 +212,58 @@ int num_sms() {
     return sms;
 }
 
+// One thread per 32-base word of a read: the four one-hot bit-planes of the
+// word, from its two packed words (first base in the high bits).
+__global__ void k_planes(DevReads R) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < R.n; r += nwarps) {
+        const int gf = R.len_gf[r];
+        const int64_t po = R.pack_off[r];
+        const int stride = (int)((R.pack_off[r + 1] - po) >> 1);
+        const int nw = (gf + 31) >> 5;
+        const uint32_t* pk = R.packed + po;
+        uint32_t* out = R.bm + 2 * po;
+        for (int w = lane; w < stride; w += 32) {
+            uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+            if (w < nw) {
+                uint32_t hi, lo;
+                // two packed words hold bases 32w .. 32w+31
+                const uint32_t u0 = pk[2 * w], u1 = pk[2 * w + 1];
+                const uint32_t b0 = __brev(u0), b1 = __brev(u1);
+                auto ev = [](uint32_t x) {
+                    x &= 0x55555555u;
+                    x = (x | (x >> 1)) & 0x33333333u;
+                    x = (x | (x >> 2)) & 0x0f0f0f0fu;
+                    x = (x | (x >> 4)) & 0x00ff00ffu;
+                    x = (x | (x >> 8)) & 0x0000ffffu;
+                    return x;
+                };
+                hi = ev(b0) | (ev(b1) << 16);
+                lo = ev(b0 >> 1) | (ev(b1 >> 1) << 16);
+                const int rem = gf - 32 * w;
+                const uint32_t valid = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
+                p0 = ~hi & ~lo & valid;
+                p1 = ~hi & lo & valid;
+                p2 = hi & ~lo & valid;
+                p3 = hi & lo & valid;
+            }
+            out[w] = p0;
+            out[stride + w] = p1;
+            out[2 * stride + w] = p2;
+            out[3 * stride + w] = p3;
+        }
+    }
+}
+
+void launch_planes(const DevReads& R, cudaStream_t s) {
+    if (R.n <= 0) return;
+    int grid = (R.n + 7) / 8;
+    const int cap = num_sms() * 16;
+    if (grid > cap) grid = cap;
+    k_planes<<<grid, 256, 0, s>>>(R);
+}
+
 void launch_pack(const DevReads& R, float t, int k, cudaStream_t s) {
     if (R.n <= 0) return;
     int grid = (R.n + kPackWarps - 1) / kPackWarps;

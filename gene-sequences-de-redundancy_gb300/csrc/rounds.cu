@@ -157,6 +157,88 @@ struct AlignArgs {
     int acc_cap;
 };
 
+// An accepted pair: the plain form absorbs the candidate at once; the batched
+// form lists the pair for the greedy-order resolution and records when a
+// tentative accepted another tentative.
+template <bool BATCH>
+__device__ __forceinline__ void on_accept(RoundState* st, const AlignArgs& A, const Pair p,
+                                          int pass) {
+    if (!BATCH) {
+        A.cluster[p.cand] = p.rep;
+        return;
+    }
+    const int slot = atomicAdd(&st->n_acc, 1);
+    if (slot < A.acc_cap) A.acc[slot] = p;
+    else st->acc_overflow = 1;
+    const uint32_t kc = A.tidx[p.cand];
+    if ((int)(kc >> 12) == pass) {
+        const int h = A.tidx[p.rep] & 0xfff, ci = kc & 0xfff;
+        atomicOr(&A.tt[h * kTTWords + (ci >> 5)], 1u << (ci & 31));
+        atomicOr(&A.ttrow[h >> 5], 1u << (h & 31));
+    }
+}
+
+// Greedy embedding in front of the alignment, one thread per queued pair:
+// walking the candidate base by base and taking, for each, the next
+// occurrence in the representative after the previous match builds a common
+// subsequence, so its length is a lower bound of the LCS.  When it reaches the
+// cutoff the pair is accepted without the bit-parallel alignment and removed
+// from its queue (rep = -1).  Any other pair is left to k_align.  Next
+// occurrences come from the representative's base bit-planes.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_greedy(DevReads R, RoundState* st, AlignArgs A) {
+    if (st->done) return;
+    if (BATCH && (st->pair_overflow || st->n_tent == 0)) return;
+    const int pass = BATCH ? st->pass : 0;
+    int counts[kAlignClasses], total = 0;
+    for (int c = 0; c < kAlignClasses; c++) {
+        counts[c] = min(st->n_pairs[c], A.seg_cap);
+        total += counts[c];
+    }
+    unsigned acc = 0;
+    unsigned long long cells = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        int cls = 0, kk = k;
+        while (kk >= counts[cls]) kk -= counts[cls++];
+        Pair* slot = const_cast<Pair*>(A.pairs) + (size_t)cls * A.seg_cap + kk;
+        const Pair p = *slot;
+        const int T = R.len_gf[p.rep], q = R.len_gf[p.cand], c = R.cut_base[p.cand];
+        if (T == 0 || c <= 0 || q < c || T < c) continue;  // trivial: k_align decides
+        const int64_t po = R.pack_off[p.rep];
+        const int stride = (int)((R.pack_off[p.rep + 1] - po) >> 1);
+        const uint32_t* planes = R.bm + 2 * po;
+        const int nw = (T + 31) >> 5;
+        const uint32_t* pq = R.packed + R.pack_off[p.cand];
+        int pos = 0, g = 0;
+        uint32_t qw = 0;
+        for (int i = 0; i < q; i++) {
+            if ((i & 15) == 0) qw = __ldg(pq + (i >> 4));
+            const uint32_t ch = (qw >> (30 - 2 * (i & 15))) & 3u;
+            const uint32_t* pl = planes + ch * stride;
+            int w = pos >> 5;
+            if (w >= nw) break;
+            uint32_t m = __ldg(pl + w) & (0xffffffffu << (pos & 31));
+            while (m == 0 && ++w < nw) m = __ldg(pl + w);
+            if (m == 0) break;
+            pos = 32 * w + __ffs(m);  // one past the match
+            if (++g >= c) break;
+            if (g + (q - 1 - i) < c) break;  // cannot reach the cutoff any more
+        }
+        if (g >= c) {
+            on_accept<BATCH>(st, A, p, pass);
+            slot->rep = -1;
+            acc++;
+            cells += (unsigned long long)T * (unsigned long long)q;
+        }
+    }
+    acc = warp_sum_i((int)acc);
+    if ((threadIdx.x & 31) == 0 && acc) {
+        if (!BATCH) atomicAdd(&st->cnt_accepted, (unsigned long long)acc);
+    }
+    // per-thread cell counts: one atomic per non-zero thread is rare enough
+    if (cells) atomicAdd(&st->cells, cells);
+}
+
 template <int G, int W, bool BATCH>
 __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundState* st, AlignArgs A,
                                                          int cls) {
@@ -188,6 +270,10 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
         const int i = *(volatile int*)&S.idx;
         if (i >= np) break;
         const Pair p = list[i];
+        if (p.rep < 0) {  // already accepted by k_greedy
+            group_bar(bar_id, bar_n);
+            continue;
+        }
         const int T = R.len_gf[p.rep], q = R.len_gf[p.cand], c = R.cut_base[p.cand];
         const int trivial = trivial_decision(T, q, c);
         if (trivial < 0) {
@@ -203,19 +289,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
             cells += (unsigned long long)T * (unsigned long long)q;
             if (ok) {
                 acc++;
-                if (!BATCH) {
-                    A.cluster[p.cand] = p.rep;
-                } else {
-                    const int slot = atomicAdd(&st->n_acc, 1);
-                    if (slot < A.acc_cap) A.acc[slot] = p;
-                    else st->acc_overflow = 1;
-                    const uint32_t kc = A.tidx[p.cand];
-                    if ((int)(kc >> 12) == pass) {  // a tentative accepted another tentative
-                        const int h = A.tidx[p.rep] & 0xfff, ci = kc & 0xfff;
-                        atomicOr(&A.tt[h * kTTWords + (ci >> 5)], 1u << (ci & 31));
-                        atomicOr(&A.ttrow[h >> 5], 1u << (h & 31));
-                    }
-                }
+                on_accept<BATCH>(st, A, p, pass);
             }
             for (int b = 0; b < 8; b++) {
                 S.ready[b] = 0;
@@ -661,10 +735,7 @@ void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain
     }
 }
 
-template <int G, int W, bool BATCH>
-void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
-    static int grid = 0;
-    if (!grid) grid = grid_for(k_align<G, W, BATCH>, kAlignThreads, 0, 8);
+AlignArgs align_args(RoundBuffers& B) {
     AlignArgs A;
     A.pairs = B.pairs;
     A.seg_cap = B.seg_cap;
@@ -675,11 +746,19 @@ void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s)
     A.ttrow = B.ttrow;
     A.acc = B.acc;
     A.acc_cap = B.acc_cap;
-    k_align<G, W, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, A, cls);
+    return A;
+}
+
+template <int G, int W, bool BATCH>
+void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
+    static int grid = 0;
+    if (!grid) grid = grid_for(k_align<G, W, BATCH>, kAlignThreads, 0, 8);
+    k_align<G, W, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
 }
 
 template <bool BATCH>
 void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s) {
+    k_greedy<BATCH><<<num_sms() * 8, 256, 0, s>>>(R, B.st, align_args(B));
     launch_align_t<1, 1, BATCH>(R, B, 0, s);
     launch_align_t<1, 2, BATCH>(R, B, 1, s);
     launch_align_t<2, 2, BATCH>(R, B, 2, s);
@@ -714,7 +793,7 @@ void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 3 + kAlignClasses;
+    if (count) *count += 4 + kAlignClasses;
 }
 
 void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,
@@ -735,7 +814,7 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 7 + kAlignClasses;
+    if (count) *count += 8 + kAlignClasses;
 }
 
 }  // namespace gsdr
