@@ -14,6 +14,7 @@
 #include "gsdr.h"
 #include "gsdr_device.cuh"
 #include "gsdr_host.h"
+#include "gsdr_testing.h"
 #include "job.h"
 
 namespace gsdr {
@@ -106,6 +107,10 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     R.n_kmer = c.take<int32_t>(n);
     R.kmer = c.take<uint32_t>((size_t)P.kmer_off[n] + 8);
     R.bm = c.take<uint32_t>(2 * (size_t)P.pack_off[n] + 8);
+    const bool bits = !drop && k <= kMaxBitsK;
+    const size_t nbw = bits ? ((size_t)1 << (2 * k)) / 32 : 0;
+    R.kbits = bits ? c.take<uint32_t>((size_t)n * nbw) : nullptr;
+    R.kextra = bits ? c.take<int32_t>(n) : nullptr;
     B.st = reinterpret_cast<RoundState*>(c.take<char>(sizeof(RoundState) + 4 * 64));
     B.cluster = c.take<int32_t>(n);
     B.remain[0] = c.take<int32_t>(n);
@@ -489,3 +494,87 @@ int gsdr_main(int argc, char** argv) {
 }
 
 }  // extern "C"
+
+// ---- testing: the alignment stage alone (include/gsdr_testing.h) ----------
+
+namespace gsdr {
+
+int Job::lcs_pairs(const int32_t* pat, const int32_t* txt, int n_pairs, int mapping, int greedy,
+                   uint8_t* accept, double* ms) {
+    if (n_pairs <= 0) return GSDR_OK;
+    std::vector<int> seen(n, 0);
+    std::vector<std::vector<Pair>> cls(kAlignClasses);
+    std::vector<int32_t> gf(n);
+    // gap-free lengths decide the class: prepare the reads first
+    JCUDA(cudaSetDevice(opts.device));
+    JCUDA(cudaMemsetAsync(R_.packed, 0, sizeof(uint32_t) * ((size_t)pack_off_[n] + 8), stream));
+    launch_pack(R_, opts.threshold, opts.word_length, stream);
+    launch_planes(R_, stream);
+    JCUDA(cudaGetLastError());
+    JCUDA(cudaMemcpyAsync(gf.data(), R_.len_gf, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, stream));
+    JCUDA(cudaStreamSynchronize(stream));
+    for (int k = 0; k < n_pairs; k++) {
+        if (pat[k] < 0 || pat[k] >= n || txt[k] < 0 || txt[k] >= n || seen[pat[k]])
+            return fail(GSDR_EINVAL, "lcs_pairs: bad or repeated pattern index");
+        seen[pat[k]] = 1;
+        cls[align_class_host((gf[pat[k]] + 31) >> 5)].push_back(Pair{txt[k], pat[k]});
+    }
+    RoundState st{};
+    for (int c = 0; c < kAlignClasses; c++) {
+        if ((int)cls[c].size() > B_.seg_cap) return fail(GSDR_EINVAL, "lcs_pairs: too many pairs");
+        st.n_pairs[c] = (int)cls[c].size();
+        if (!cls[c].empty())
+            JCUDA(cudaMemcpyAsync(B_.pairs + (size_t)c * B_.seg_cap, cls[c].data(),
+                                  sizeof(Pair) * cls[c].size(), cudaMemcpyHostToDevice, stream));
+    }
+    st.pass = 1;
+    st.n_tent = 1;
+    st.R = 1;
+    JCUDA(cudaMemcpyAsync(B_.st, &st, sizeof(st), cudaMemcpyHostToDevice, stream));
+    JCUDA(cudaMemsetAsync(B_.st + 1, 0, 64 * sizeof(int), stream));
+    JCUDA(cudaMemsetAsync(B_.cluster, 0xff, sizeof(int32_t) * n, stream));
+    JCUDA(cudaMemsetAsync(B_.tidx, 0xff, sizeof(uint32_t) * n, stream));
+    JCUDA(cudaEventRecord(ev_[2], stream));
+    launch_align_stage(R_, B_, mapping == 1, greedy != 0, stream);
+    JCUDA(cudaGetLastError());
+    JCUDA(cudaEventRecord(ev_[3], stream));
+    JCUDA(cudaMemcpyAsync(h_state_, B_.st, sizeof(RoundState), cudaMemcpyDeviceToHost, stream));
+    std::vector<int32_t> cl(n);
+    JCUDA(cudaMemcpyAsync(cl.data(), B_.cluster, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, stream));
+    JCUDA(cudaStreamSynchronize(stream));
+    if (h_state_->error) return fail(GSDR_ETIMEOUT, "lcs_pairs: a device-side wait gave up");
+    if (mapping == 1) {
+        const int na = h_state_->n_acc;
+        if (na > B_.acc_cap) return fail(GSDR_ENOMEM, "lcs_pairs: accept list overflow");
+        std::vector<Pair> acc(na);
+        if (na)
+            JCUDA(cudaMemcpy(acc.data(), B_.acc, sizeof(Pair) * na, cudaMemcpyDeviceToHost));
+        for (const Pair& p : acc) cl[p.cand] = p.rep;
+    }
+    for (int k = 0; k < n_pairs; k++) accept[k] = cl[pat[k]] == txt[k] ? 1 : 0;
+    float f = 0;
+    cudaEventElapsedTime(&f, ev_[2], ev_[3]);
+    if (ms) *ms = f;
+    return GSDR_OK;
+}
+
+}  // namespace gsdr
+
+extern "C" int gsdr_lcs_decide(const char* bytes, int64_t n_bytes, const int64_t* off,
+                               const int32_t* len, int32_t n_seq, const int32_t* pat,
+                               const int32_t* txt, int32_t n_pairs, float t, int32_t mapping,
+                               int32_t greedy, uint8_t* accept, double* ms) {
+    if (!pat || !txt || (!accept && n_pairs > 0) || n_pairs < 0)
+        return fail(GSDR_EINVAL, "gsdr_lcs_decide: null argument");
+    gsdr_reads r{bytes, n_bytes, off, len, n_seq};
+    gsdr_opts o;
+    gsdr_default_opts(&o);
+    o.threshold = t;
+    o.drop = 1;
+    o.batch = 1;
+    Job job;
+    int rc = job.init(&r, &o);
+    if (!rc) rc = job.upload(&r);
+    if (!rc) rc = job.lcs_pairs(pat, txt, n_pairs, mapping, greedy, accept, ms);
+    return rc;
+}

@@ -23,6 +23,7 @@ constexpr int kMaxPatternWords = 1024;  // 8 warps x 32 lanes x 4 words: 32768 g
 constexpr int kAlignClasses = 6;        // pattern length classes of the alignment kernels
 constexpr int kMaxBatch = 1024;         // tentative representatives per batched pass
 constexpr int kTTWords = kMaxBatch / 32;
+constexpr int kMaxBitsK = 6;            // k-mer presence bitmaps for k <= 6 (4^k bits per read)
 
 struct DevReads {
     int32_t n;
@@ -44,6 +45,11 @@ struct DevReads {
     // at bm[2*pack_off[i] + c*(pack_off[i+1]-pack_off[i])/2]; bit b of word w
     // is set iff base 32w+b equals c (bits past the read are zero)
     uint32_t* bm;
+    // k <= kMaxBitsK: presence bitmap of the k-mers with a non-zero stored
+    // multiplicity (4^k bits per read, read i at kbits[i * 4^k/32]) and the
+    // multiplicity excess sum(count) - #distinct over those k-mers
+    uint32_t* kbits;
+    int32_t* kextra;
 };
 
 // Per-job round state, in device memory; kernels read their work sizes here so
@@ -111,6 +117,11 @@ void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cud
 // (optional) receives events around the filter and alignment stages.
 void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity,
                         cudaStream_t s, long long* count, cudaEvent_t* ev4);
+// Only the alignment stage over the queued pairs (st->n_pairs), with the
+// plain or the batched warp grouping, optionally after the greedy bound.
+void launch_align_stage(const DevReads& R, RoundBuffers& B, bool batched_mapping, bool greedy,
+                        cudaStream_t s);
+int align_class_host(int words);
 // One batched pass (select, filter, align, resolve, compact, advance).
 void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,
                        long long* count, cudaEvent_t* ev4);

@@ -23,6 +23,10 @@ public:
     int run();
     // Device -> host copy of the cluster array (synchronous).
     int download(int32_t* cluster);
+    // Testing: decisions of the alignment stage on given (pattern, text) pairs
+    // (read indices); the job must have been initialised with drop = 1.
+    int lcs_pairs(const int32_t* pat, const int32_t* txt, int n_pairs, int mapping, int greedy,
+                  uint8_t* accept, double* ms);
     // Device bytes this job needs for its inputs (admission by footprint).
     static int64_t footprint(const gsdr_reads* reads, const gsdr_opts* opts);
 

@@ -141,21 +141,24 @@ __global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, i
 template <int K>
 __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
     constexpr int NB = 1 << (2 * K);
+    constexpr bool BITS = K <= kMaxBitsK;
+    constexpr int NBW = BITS ? NB / 32 : 1;
     extern __shared__ __align__(16) uint32_t sm[];
     uint32_t* hist = sm;
     uint16_t* list = reinterpret_cast<uint16_t*>(sm + NB);
-    __shared__ int nlist;
+    __shared__ uint32_t bits[NBW];
+    __shared__ int nlist, sumcnt;
     for (int i = threadIdx.x; i < NB; i += blockDim.x) hist[i] = 0;
-    if (threadIdx.x == 0) nlist = 0;
+    for (int i = threadIdx.x; i < NBW; i += blockDim.x) bits[i] = 0;
+    if (threadIdx.x == 0) {
+        nlist = 0;
+        sumcnt = 0;
+    }
     __syncthreads();
     for (int r = blockIdx.x; r < R.n; r += gridDim.x) {
         const int gf = R.len_gf[r];
         const int nk = gf - K + 1;
         uint32_t* out = R.kmer + R.kmer_off[r];
-        if (nk <= 0) {
-            if (threadIdx.x == 0) R.n_kmer[r] = 0;
-            continue;
-        }
         const uint32_t* pk = R.packed + R.pack_off[r];
         for (int p = threadIdx.x; p < nk; p += blockDim.x) {
             const int w = p >> 4, o = p & 15;
@@ -166,17 +169,37 @@ __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
         }
         __syncthreads();
         const int nl = nlist;
+        int my_sum = 0;
         for (int s = threadIdx.x; s < nl; s += blockDim.x) {
             const uint32_t km = list[s];
-            const uint32_t c = hist[km];
-            out[s] = (km << 16) | (c & 0xffffu);
+            const uint32_t c = hist[km] & 0xffffu;  // the reference's u16 multiplicity
+            out[s] = (km << 16) | c;
             hist[km] = 0;
+            if (BITS && c) {
+                atomicOr(&bits[km >> 5], 1u << (km & 31));
+                my_sum += (int)c - 1;
+            }
         }
         const int padded = (nl + 3) & ~3;
         for (int s = nl + threadIdx.x; s < padded; s += blockDim.x) out[s] = 0u;
-        if (threadIdx.x == 0) R.n_kmer[r] = nl;
+        if (BITS) {
+            my_sum = warp_sum(my_sum);
+            if ((threadIdx.x & 31) == 0 && my_sum) atomicAdd(&sumcnt, my_sum);
+        }
         __syncthreads();
-        if (threadIdx.x == 0) nlist = 0;
+        if (BITS) {
+            uint32_t* ob = R.kbits + (size_t)r * NBW;
+            for (int i = threadIdx.x; i < NBW; i += blockDim.x) {
+                ob[i] = bits[i];
+                bits[i] = 0;
+            }
+        }
+        if (threadIdx.x == 0) {
+            R.n_kmer[r] = nl;
+            if (BITS) R.kextra[r] = sumcnt;
+            nlist = 0;
+            sumcnt = 0;
+        }
         __syncthreads();
     }
 }

@@ -53,9 +53,16 @@ __device__ __forceinline__ bool prefilter_pass(const int4 a, const int4 b, int c
     return !(s < cut);
 }
 
-// Alignment class of a pattern of `words` 32-base words (warps x words/lane):
-// 0: <=32 (1x1), 1: <=64 (1x2), 2: <=128 (2x2), 3: <=256 (4x2), 4: <=512 (8x2),
-// 5: <=1024 (8x4).
+// Alignment class of a pattern of `words` 32-base words; the classes hold the
+// same word counts in both forms, as warps x words per lane:
+//   class            0       1       2        3        4        5
+//   words          <=32    <=64   <=128    <=256    <=512   <=1024
+//   plain form      1x1     1x2     2x2      4x2      8x2      8x4
+//   batched form    1x1     1x2     1x4      1x8      2x8      4x8
+// The plain form waits for every round's longest pair, so it spreads a pattern
+// over more warps (shorter per-base chain); the batched form has many pairs in
+// flight and packs each pattern into as few warps as it can (fewer
+// instructions per DP cell, no hand-offs between warps).
 __device__ __forceinline__ int align_class(int words) {
     return words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 256 ? 3
                                                              : words <= 512 ? 4 : 5;
@@ -76,6 +83,9 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
                                                            const int32_t* __restrict__ remain,
                                                            Pair* pairs, int seg_cap) {
     extern __shared__ __align__(16) uint16_t table[];
+    constexpr bool BITS = !DROP && K <= kMaxBitsK;
+    constexpr int NBW = BITS ? (1 << (2 * K)) / 32 : 4;
+    __shared__ __align__(16) uint32_t rbits[NBW];
     if (st->done) return;
     const int rep = st->rep;
     const int n = st->n_remain;
@@ -92,8 +102,11 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
             const uint32_t c = v & 0xffffu;
             if (c) table[v >> 16] = (uint16_t)c;  // kernel_makeTable: only order > 0
         }
+        if (BITS)
+            for (int i = threadIdx.x; i < NBW; i += blockDim.x) rbits[i] = R.kbits[(size_t)rep * NBW + i];
         __syncthreads();
     }
+    const int rep_extra = BITS ? R.kextra[rep] : 0;
     const int lane = threadIdx.x & 31;
     const int4 crep = R.comp[rep];
     unsigned n_pf = 0, n_wf = 0, n_al = 0;
@@ -107,23 +120,43 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
         // kernel_preFilter (func.cu:738-754); lossless, so also used in drop mode.
         if (!prefilter_pass(crep, R.comp[q], R.cut_base[q])) continue;
         if (!DROP) {
-            // kernel_filter (func.cu:803-826): sum over distinct k-mers of
-            // min(count in representative, count in candidate).
+            // kernel_filter (func.cu:803-826): S = sum over distinct k-mers of
+            // min(count in representative, count in candidate), compared with
+            // the candidate's word cutoff.
             n_wf++;
-            const int ne4 = (R.n_kmer[q] + 3) >> 2;
-            const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
-            int sum = 0;
-#pragma unroll 4
-            for (int i = lane; i < ne4; i += 32) {
-                const uint4 v = __ldcs(e4 + i);
-                sum += min((uint32_t)table[v.x >> 16], v.x & 0xffffu);
-                sum += min((uint32_t)table[v.y >> 16], v.y & 0xffffu);
-                sum += min((uint32_t)table[v.z >> 16], v.z & 0xffffu);
-                sum += min((uint32_t)table[v.w >> 16], v.w & 0xffffu);
+            const int cw = R.cut_word[q];
+            bool decided = false, pass = false;
+            if (BITS) {
+                // D = shared k-mers (non-zero counts) bounds S: D <= S <= D + min(excesses)
+                const uint4 cb = __ldcs(reinterpret_cast<const uint4*>(R.kbits + (size_t)q * NBW) + lane % (NBW / 4));
+                int d = 0;
+                if (lane < NBW / 4) {
+                    const uint4 rb = reinterpret_cast<const uint4*>(rbits)[lane];
+                    d = __popc(cb.x & rb.x) + __popc(cb.y & rb.y) + __popc(cb.z & rb.z) +
+                        __popc(cb.w & rb.w);
+                }
+                d = warp_sum_i(d);
+                bytes += 4ull * NBW;
+                if (d >= cw) decided = pass = true;
+                else if (d + min(R.kextra[q], rep_extra) < cw) decided = true;
             }
-            bytes += 16ull * ne4;
-            sum = warp_sum_i(sum);
-            if (sum < R.cut_word[q]) continue;
+            if (!decided) {
+                const int ne4 = (R.n_kmer[q] + 3) >> 2;
+                const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
+                int sum = 0;
+#pragma unroll 4
+                for (int i = lane; i < ne4; i += 32) {
+                    const uint4 v = __ldcs(e4 + i);
+                    sum += min((uint32_t)table[v.x >> 16], v.x & 0xffffu);
+                    sum += min((uint32_t)table[v.y >> 16], v.y & 0xffffu);
+                    sum += min((uint32_t)table[v.z >> 16], v.z & 0xffffu);
+                    sum += min((uint32_t)table[v.w >> 16], v.w & 0xffffu);
+                }
+                bytes += 16ull * ne4;
+                sum = warp_sum_i(sum);
+                pass = !(sum < cw);
+            }
+            if (!pass) continue;
         }
         n_al++;
         if (lane == 0) push_pair(st, pairs, seg_cap, R, rep, q);
@@ -204,25 +237,48 @@ __global__ void __launch_bounds__(256) k_greedy(DevReads R, RoundState* st, Alig
         const Pair p = *slot;
         const int T = R.len_gf[p.rep], q = R.len_gf[p.cand], c = R.cut_base[p.cand];
         if (T == 0 || c <= 0 || q < c || T < c) continue;  // trivial: k_align decides
+        // The walk is sequential, and the longest walk of a pass delays the
+        // whole pass: long candidates go to the (lane-parallel) alignment
+        // unless the representative is long enough for an embedding.
+        if (q > 4096 || (q > 2048 && T < 3 * c)) continue;
         const int64_t po = R.pack_off[p.rep];
         const int stride = (int)((R.pack_off[p.rep + 1] - po) >> 1);
         const uint32_t* planes = R.bm + 2 * po;
         const int nw = (T + 31) >> 5;
         const uint32_t* pq = R.packed + R.pack_off[p.cand];
-        int pos = 0, g = 0;
+        // The four plane words of the current 32-base text word stay in
+        // registers; a new word is loaded only when the match position
+        // crosses into it.  The walk also stops when reaching the cutoff has
+        // become impossible (too little text or candidate left) or, after
+        // 256 matches, when the text used per match so far projects well
+        // past the end: stopping only hands the pair to the alignment.
+        int pos = 0, g = 0, wcur = -1;
+        uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
         uint32_t qw = 0;
         for (int i = 0; i < q; i++) {
             if ((i & 15) == 0) qw = __ldg(pq + (i >> 4));
             const uint32_t ch = (qw >> (30 - 2 * (i & 15))) & 3u;
-            const uint32_t* pl = planes + ch * stride;
+            uint32_t m = 0;
             int w = pos >> 5;
-            if (w >= nw) break;
-            uint32_t m = __ldg(pl + w) & (0xffffffffu << (pos & 31));
-            while (m == 0 && ++w < nw) m = __ldg(pl + w);
-            if (m == 0) break;
+            while (w < nw) {
+                if (w != wcur) {
+                    p0 = __ldg(planes + w);
+                    p1 = __ldg(planes + stride + w);
+                    p2 = __ldg(planes + 2 * stride + w);
+                    p3 = __ldg(planes + 3 * stride + w);
+                    wcur = w;
+                }
+                m = ch == 0 ? p0 : ch == 1 ? p1 : ch == 2 ? p2 : p3;
+                if (32 * w < pos) m &= 0xffffffffu << (pos & 31);
+                if (m) break;
+                w++;
+            }
+            if (!m) break;
             pos = 32 * w + __ffs(m);  // one past the match
             if (++g >= c) break;
-            if (g + (q - 1 - i) < c) break;  // cannot reach the cutoff any more
+            const int need = c - g;
+            if (g + (q - 1 - i) < c || T - pos < need) break;
+            if (g >= 256 && (long long)pos * need > 5ll * (T - pos) * g / 4) break;
         }
         if (g >= c) {
             on_accept<BATCH>(st, A, p, pass);
@@ -757,14 +813,21 @@ void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s)
 }
 
 template <bool BATCH>
-void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s) {
-    k_greedy<BATCH><<<num_sms() * 8, 256, 0, s>>>(R, B.st, align_args(B));
+void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bool greedy = true) {
+    if (greedy) k_greedy<BATCH><<<num_sms() * 8, 256, 0, s>>>(R, B.st, align_args(B));
     launch_align_t<1, 1, BATCH>(R, B, 0, s);
     launch_align_t<1, 2, BATCH>(R, B, 1, s);
-    launch_align_t<2, 2, BATCH>(R, B, 2, s);
-    launch_align_t<4, 2, BATCH>(R, B, 3, s);
-    launch_align_t<8, 2, BATCH>(R, B, 4, s);
-    launch_align_t<8, 4, BATCH>(R, B, 5, s);
+    if constexpr (BATCH) {
+        launch_align_t<1, 4, BATCH>(R, B, 2, s);
+        launch_align_t<1, 8, BATCH>(R, B, 3, s);
+        launch_align_t<2, 8, BATCH>(R, B, 4, s);
+        launch_align_t<4, 8, BATCH>(R, B, 5, s);
+    } else {
+        launch_align_t<2, 2, BATCH>(R, B, 2, s);
+        launch_align_t<4, 2, BATCH>(R, B, 3, s);
+        launch_align_t<8, 2, BATCH>(R, B, 4, s);
+        launch_align_t<8, 4, BATCH>(R, B, 5, s);
+    }
 }
 
 }  // namespace
@@ -794,6 +857,17 @@ void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity
     k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
     if (count) *count += 4 + kAlignClasses;
+}
+
+void launch_align_stage(const DevReads& R, RoundBuffers& B, bool batched_mapping, bool greedy,
+                        cudaStream_t s) {
+    if (batched_mapping) launch_align_classes<true>(R, B, s, greedy);
+    else launch_align_classes<false>(R, B, s, greedy);
+}
+
+int align_class_host(int words) {
+    return words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 256 ? 3
+                                                             : words <= 512 ? 4 : 5;
 }
 
 void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,

@@ -146,6 +146,9 @@ def lib():
         L.gsdr_job_run.argtypes = [C.c_void_p, P(Stats)]
         L.gsdr_job_cluster.argtypes = [C.c_void_p, C.c_void_p]
         L.gsdr_job_free.argtypes = [C.c_void_p]
+        L.gsdr_lcs_decide.argtypes = [C.c_char_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int32,
+                                      C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_int32,
+                                      C.c_int32, C.c_void_p, C.POINTER(C.c_double)]
         L.gsdr_strerror.restype = C.c_char_p
         L.gsdr_last_error.restype = C.c_char_p
         _lib = L
@@ -328,6 +331,25 @@ def cluster_bytes(data: bytes, **kw) -> bytes:
         return f.format(cl)
     finally:
         f.close()
+
+
+def lcs_decide(seqs, pairs, t, mapping=0, greedy=0):
+    """Alignment stage alone (include/gsdr_testing.h): seqs is a list of
+    byte strings, pairs a list of (pattern, text) indices (each pattern at
+    most once).  Returns (accept array, device ms)."""
+    data = b"".join(seqs)
+    off = np.zeros(len(seqs), dtype=np.int64)
+    if len(seqs) > 1:
+        off[1:] = np.cumsum([len(x) for x in seqs])[:-1]
+    ln = np.array([len(x) for x in seqs], dtype=np.int32)
+    pat = np.ascontiguousarray([p for p, _ in pairs], dtype=np.int32)
+    txt = np.ascontiguousarray([x for _, x in pairs], dtype=np.int32)
+    acc = np.zeros(len(pairs), dtype=np.uint8)
+    ms = C.c_double()
+    _check(lib().gsdr_lcs_decide(data, len(data), off.ctypes.data, ln.ctypes.data, len(seqs),
+                                 pat.ctypes.data, txt.ctypes.data, len(pairs), C.c_float(t),
+                                 mapping, greedy, acc.ctypes.data, C.byref(ms)))
+    return acc, ms.value
 
 
 def main(argv) -> int:

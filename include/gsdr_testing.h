@@ -1,0 +1,29 @@
+/* gsdr_testing.h -- kernel-level entry points for tests and benchmarks.
+ *
+ * No counterpart in the reference, which only exposes the whole program.
+ * gsdr_lcs_decide runs the library's alignment stage on a caller-given list
+ * of (pattern, text) pairs: each decision is the reference's kernel_align
+ * test (cuda-version/func.cu:828-999), LCS(pattern, text) >= ceil(len * t)
+ * over gap-free bases, with len the pattern's raw length.
+ */
+#ifndef GSDR_TESTING_H
+#define GSDR_TESTING_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Sequences: seq i is bytes[off[i] .. off[i] + len[i]).  Pair k decides
+ * pattern pat[k] against text txt[k]; a pattern index may appear in at most
+ * one pair.  mapping: 0 = the plain form's warp grouping, 1 = the batched
+ * form's; greedy: 1 = try the greedy-embedding lower bound first.
+ * accept[k] receives 0/1; *ms the device time of the alignment stage. */
+int gsdr_lcs_decide(const char* bytes, int64_t n_bytes, const int64_t* off, const int32_t* len,
+                    int32_t n_seq, const int32_t* pat, const int32_t* txt, int32_t n_pairs,
+                    float t, int32_t mapping, int32_t greedy, uint8_t* accept, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

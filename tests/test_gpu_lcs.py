@@ -1,0 +1,112 @@
+"""Alignment kernels alone against the oracle's LCS: the decision
+LCS(pattern, text) >= ceil(len(pattern) * t) (kernel_align,
+cuda-version/func.cu:828-999) for random, mutated and repetitive pairs in
+every length class, with both warp groupings and with the greedy bound."""
+import numpy as np
+import pytest
+
+import gsdr
+import oracle_binding as orc
+
+pytestmark = pytest.mark.gpu
+
+CODES = np.frombuffer(b"ACGT", dtype=np.uint8)
+
+
+def rand_seq(rng, n):
+    return CODES[rng.integers(0, 4, n)].tobytes()
+
+
+def mutate(rng, s, rate, indel=0.2):
+    out = bytearray()
+    for ch in s:
+        r = rng.random()
+        if r < rate * (1 - indel):
+            out.append(int(CODES[rng.integers(0, 4)]))
+        elif r < rate * (1 - indel / 2):
+            continue
+        elif r < rate:
+            out.append(ch)
+            out.append(int(CODES[rng.integers(0, 4)]))
+        else:
+            out.append(ch)
+    return bytes(out)
+
+
+def expected(seqs, pairs, t):
+    lens = np.array([len(s) for s in seqs], dtype=np.int32)
+    _, base, _ = orc.cutoffs(lens, t, 6)
+    out = []
+    for p, x in pairs:
+        a = np.frombuffer(seqs[p].translate(bytes.maketrans(b"ACGT", b"\0\1\2\3")), dtype=np.uint8)
+        b = np.frombuffer(seqs[x].translate(bytes.maketrans(b"ACGT", b"\0\1\2\3")), dtype=np.uint8)
+        if len(b) == 0:
+            out.append(0)
+            continue
+        out.append(1 if orc.lcs(a, b) >= base[p] else 0)
+    return np.array(out, dtype=np.uint8)
+
+
+def build_case(rng, n_pairs, qlen, tlen, kind):
+    seqs, pairs = [], []
+    for _ in range(n_pairs):
+        q = int(rng.integers(*qlen))
+        T = int(rng.integers(*tlen))
+        if kind == "random":
+            a, b = rand_seq(rng, q), rand_seq(rng, T)
+        elif kind == "mutated":
+            b = rand_seq(rng, T)
+            a = mutate(rng, b[:q], rng.uniform(0.0, 0.12))
+        elif kind == "repeats":
+            unit = rand_seq(rng, int(rng.integers(1, 5)))
+            b = (unit * (T // len(unit) + 1))[:T]
+            a = mutate(rng, (unit * (q // len(unit) + 1))[:q], 0.03)
+        else:  # embedding: short pattern, long text
+            a, b = rand_seq(rng, q), rand_seq(rng, T)
+        seqs.append(b)
+        seqs.append(a)
+        pairs.append((len(seqs) - 1, len(seqs) - 2))
+    return seqs, pairs
+
+
+@pytest.mark.parametrize("mapping", [0, 1])
+@pytest.mark.parametrize("greedy", [0, 1])
+@pytest.mark.parametrize("qlen,tlen,kind", [
+    ((20, 1000), (20, 1200), "mutated"),        # classes 0-1
+    ((1000, 4000), (1000, 4500), "mutated"),    # classes 1-3
+    ((4000, 9000), (4000, 9500), "mutated"),    # classes 3-4
+    ((16000, 20000), (16000, 21000), "mutated"),  # class 5
+    ((300, 2500), (9000, 10000), "embed"),      # short pattern, long text
+    ((1500, 5000), (3000, 10000), "random"),    # near-threshold rejects
+    ((50, 3000), (50, 3000), "repeats"),
+])
+def test_lcs_decisions(mapping, greedy, qlen, tlen, kind):
+    rng = np.random.default_rng(hash((qlen, tlen, kind)) & 0xffff)
+    n = 24 if qlen[0] >= 16000 else 120
+    seqs, pairs = build_case(rng, n, qlen, tlen, kind)
+    for t in (0.80, 0.95):
+        got, ms = gsdr.lcs_decide(seqs, pairs, t, mapping=mapping, greedy=greedy)
+        want = expected(seqs, pairs, t)
+        bad = np.nonzero(got != want)[0]
+        assert len(bad) == 0, f"t={t}: {len(bad)} of {len(pairs)} differ, first {bad[:5]}"
+
+
+def test_lcs_edge_lengths():
+    rng = np.random.default_rng(7)
+    seqs, pairs = [], []
+    # lengths around word / lane / class boundaries, and N-containing patterns
+    for q in (1, 2, 15, 16, 17, 31, 32, 33, 63, 64, 65, 1023, 1024, 1025, 2048, 2049, 4096,
+              4097, 8192, 8193, 16384, 16385):
+        b = rand_seq(rng, q + int(rng.integers(0, 40)))
+        a = mutate(rng, b[:q], 0.03)
+        seqs.append(b)
+        seqs.append(a)
+        pairs.append((len(seqs) - 1, len(seqs) - 2))
+    b = rand_seq(rng, 500)
+    seqs.append(b)
+    seqs.append(b[:200] + b"NNNNNNNNNN" + b[200:400])
+    pairs.append((len(seqs) - 1, len(seqs) - 2))
+    for mapping in (0, 1):
+        for t in (0.8, 0.9, 0.95):
+            got, _ = gsdr.lcs_decide(seqs, pairs, t, mapping=mapping, greedy=1)
+            np.testing.assert_array_equal(got, expected(seqs, pairs, t))
