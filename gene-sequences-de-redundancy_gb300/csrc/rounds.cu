@@ -363,6 +363,66 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
     }
 }
 
+// The four single-warp classes of the batched grouping (1x1, 1x2, 1x4, 1x8)
+// in one launch: a warp takes pairs from one queue that runs through classes
+// 3, 2, 1, 0 in that order, so the longest pairs start first and the short
+// ones fill in behind them (one kernel tail per pass instead of four).
+__global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, RoundState* st,
+                                                                   AlignArgs A, int* work) {
+    __shared__ SysGroup groups[kAlignThreads / 32];
+    if (st->done) return;
+    if (st->pair_overflow || st->n_tent == 0) return;
+    int cnt[4], total = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        cnt[c] = min(st->n_pairs[3 - c], A.seg_cap);
+        total += cnt[c];
+    }
+    if (total <= 0) return;
+    const int pass = st->pass;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    SysGroup& S = groups[warp];
+    unsigned long long cells = 0;
+    while (true) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(work, 1);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= total) break;
+        int q4 = 0;
+        while (i >= cnt[q4]) i -= cnt[q4++];
+        const int cls = 3 - q4;
+        const Pair p = A.pairs[(size_t)cls * A.seg_cap + i];
+        if (p.rep < 0) continue;  // already accepted by k_greedy
+        const int T = R.len_gf[p.rep], q = R.len_gf[p.cand], c = R.cut_base[p.cand];
+        int ok = trivial_decision(T, q, c);
+        if (ok < 0) {
+            if (lane == 0) {
+                S.ready[0] = 0;
+                S.consumed[0] = 0;
+                S.stop = 0;
+                S.result = 0;
+                S.error = 0;
+            }
+            __syncwarp();
+            const uint32_t* pq = R.packed + R.pack_off[p.cand];
+            const uint32_t* pt = R.packed + R.pack_off[p.rep];
+            switch (cls) {
+                case 0: lcs_sys_pair<1>(S, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 1: lcs_sys_pair<2>(S, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 2: lcs_sys_pair<4>(S, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                default: lcs_sys_pair<8>(S, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+            }
+            __syncwarp();
+            ok = *(volatile int*)&S.error ? 0 : *(volatile int*)&S.result;
+        }
+        if (lane == 0) {
+            cells += (unsigned long long)T * (unsigned long long)q;
+            if (ok) on_accept<true>(st, A, p, pass);
+        }
+    }
+    if (lane == 0 && cells) atomicAdd(&st->cells, cells);
+}
+
 __global__ void k_compact(RoundState* st, const int32_t* __restrict__ remain_in,
                           int32_t* __restrict__ remain_out, const int32_t* __restrict__ cluster) {
     if (st->done) return;
@@ -397,6 +457,7 @@ __device__ void reset_align_counters(RoundState* st, int* align_work) {
         st->n_pairs[c] = 0;
         align_work[c] = 0;
     }
+    align_work[6] = 0;  // k_align_single's shared queue
 }
 
 __global__ void k_advance(RoundState* st, int32_t* cluster, int* align_work) {
@@ -725,7 +786,7 @@ __global__ void k_init(RoundState* st, int32_t* cluster, int32_t* remain, uint32
         s.R = 1;
         s.R_max = r_max;
         *st = s;
-        for (int c = 0; c < kAlignClasses; c++) align_work[c] = 0;
+        for (int c = 0; c < kAlignClasses + 1; c++) align_work[c] = 0;
     }
 }
 
@@ -815,11 +876,16 @@ void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s)
 template <bool BATCH>
 void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bool greedy = true) {
     if (greedy) k_greedy<BATCH><<<num_sms() * 8, 256, 0, s>>>(R, B.st, align_args(B));
-    launch_align_t<1, 1, BATCH>(R, B, 0, s);
-    launch_align_t<1, 2, BATCH>(R, B, 1, s);
+    if constexpr (!BATCH) {
+        launch_align_t<1, 1, BATCH>(R, B, 0, s);
+        launch_align_t<1, 2, BATCH>(R, B, 1, s);
+    }
     if constexpr (BATCH) {
-        launch_align_t<1, 4, BATCH>(R, B, 2, s);
-        launch_align_t<1, 8, BATCH>(R, B, 3, s);
+        static int grid = 0;
+        if (!grid) grid = grid_for(k_align_single, kAlignThreads, 0, 8);
+        // the single-warp classes share work counter slot 6
+        k_align_single<<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B),
+                                                      reinterpret_cast<int*>(B.st + 1) + 6);
         launch_align_t<2, 8, BATCH>(R, B, 4, s);
         launch_align_t<4, 8, BATCH>(R, B, 5, s);
     } else {
@@ -888,7 +954,7 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 8 + kAlignClasses;
+    if (count) *count += 8 + kAlignClasses - 3;
 }
 
 }  // namespace gsdr

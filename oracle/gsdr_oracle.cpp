@@ -521,7 +521,12 @@ void orc_cutoffs(const int* len, int n, float t, int k, int* word, int* base, in
     for (int i = 0; i < n; i++) orc::cutoffs(len[i], t, k, word[i], base[i], pigeon[i]);
 }
 
+// LCS of two gap-free code sequences (values 0..3); -1 for any other value.
 int orc_lcs(const uint8_t* a, int na, const uint8_t* b, int nb, int mode) {
+    for (int i = 0; i < na; i++)
+        if (a[i] > 3) return -1;
+    for (int i = 0; i < nb; i++)
+        if (b[i] > 3) return -1;
     return mode == 0 ? orc::lcs_dp(a, na, b, nb) : orc::lcs_bits(a, na, b, nb);
 }
 
