@@ -149,6 +149,9 @@ def lib():
         L.gsdr_lcs_decide.argtypes = [C.c_char_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int32,
                                       C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_int32,
                                       C.c_int32, C.c_void_p, C.POINTER(C.c_double)]
+        L.gsdr_lcs_decide_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                              C.c_float, C.c_void_p, C.c_void_p]
         L.gsdr_strerror.restype = C.c_char_p
         L.gsdr_last_error.restype = C.c_char_p
         _lib = L
@@ -350,6 +353,13 @@ def lcs_decide(seqs, pairs, t, mapping=0, greedy=0):
                                  pat.ctypes.data, txt.ctypes.data, len(pairs), C.c_float(t),
                                  mapping, greedy, acc.ctypes.data, C.byref(ms)))
     return acc, ms.value
+
+
+def lcs_decide_noalloc(d_packed, d_pack_off, d_len_raw, d_len_gf, n_seq, d_pat, d_txt,
+                       n_pairs, t, d_accept, stream=None):
+    """gsdr_lcs_decide_noalloc on device pointers (integers); raises on error."""
+    _check(lib().gsdr_lcs_decide_noalloc(d_packed, d_pack_off, d_len_raw, d_len_gf, n_seq,
+                                         d_pat, d_txt, n_pairs, C.c_float(t), d_accept, stream))
 
 
 def main(argv) -> int:

@@ -136,6 +136,36 @@ int gsdr_job_run(gsdr_job* job, gsdr_stats* stats);
 int gsdr_job_cluster(gsdr_job* job, int32_t* cluster);
 void gsdr_job_free(gsdr_job* job);
 
+/* The alignment-stage decision for callers that cannot allocate device memory.
+ * No counterpart in the reference.  Some callers own every device allocation:
+ * code inside a framework's memory pool or a plug-in that must not grow the
+ * process's device footprint.  This entry point calls no cudaMalloc, cudaFree
+ * or allocating library routine.  The caller passes device buffers for the
+ * inputs and the output.  The work space lives in one fixed array of the
+ * library of about 1.3 MB, which every GPU that loads the library holds until
+ * the process exits.  That bounds the work per call: at most
+ * GSDR_NOALLOC_MAX_PAIRS pairs over at most GSDR_NOALLOC_MAX_SEQS sequences of
+ * at most 32768 gap-free bases; larger calls return GSDR_EINVAL.
+ *
+ * Inputs (device memory): packed 2-bit sequences (16 bases per uint32, first
+ * base in bits 31:30, sequence i from word d_pack_off[i], readable one word
+ * past its last base word), the raw length (for the cutoff ceil(len * t)) and
+ * gap-free length of each sequence, and n_pairs (pattern, text) index pairs.
+ * A pattern index may appear in at most one pair.  Output: d_accept[k] = 1 iff
+ * LCS(pattern, text) >= ceil(raw length of the pattern * t).
+ *
+ * The first call on a device, made with that device current, looks up the
+ * array's device address; make that first call before any stream capture.
+ * Every call reuses the same array and clears what it needs at the start, so
+ * calls that overlap on the GPU race and give undefined results.  The call
+ * returns after the work on `stream` (a cudaStream_t, or NULL) has finished. */
+#define GSDR_NOALLOC_MAX_PAIRS 16384
+#define GSDR_NOALLOC_MAX_SEQS 65536
+int gsdr_lcs_decide_noalloc(const uint32_t* d_packed, const int64_t* d_pack_off,
+                            const int32_t* d_len_raw, const int32_t* d_len_gf, int32_t n_seq,
+                            const int32_t* d_pat, const int32_t* d_txt, int32_t n_pairs,
+                            float t, uint8_t* d_accept, void* stream);
+
 /* main (cuda-version/main.cu:3-36): the `cluster` command line.  Returns the
  * process exit status (0 also for the usage exit, as in the reference). */
 int gsdr_main(int argc, char** argv);
