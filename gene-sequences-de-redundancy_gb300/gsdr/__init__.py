@@ -152,6 +152,15 @@ def lib():
         L.gsdr_lcs_decide_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                               C.c_float, C.c_void_p, C.c_void_p]
+        L.gsdr_server_create.argtypes = [C.POINTER(ServerOpts), C.POINTER(C.c_void_p)]
+        L.gsdr_server_submit.argtypes = [C.c_void_p, C.c_char_p, C.c_int64, C.c_float,
+                                         C.POINTER(C.c_int64)]
+        L.gsdr_server_wait.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.gsdr_server_result.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                         C.POINTER(C.c_int64), C.c_void_p, C.POINTER(C.c_int32)]
+        L.gsdr_server_release.argtypes = [C.c_void_p, C.c_int64]
+        L.gsdr_server_destroy.argtypes = [C.c_void_p]
         L.gsdr_strerror.restype = C.c_char_p
         L.gsdr_last_error.restype = C.c_char_p
         _lib = L
@@ -360,6 +369,55 @@ def lcs_decide_noalloc(d_packed, d_pack_off, d_len_raw, d_len_gf, n_seq, d_pat, 
     """gsdr_lcs_decide_noalloc on device pointers (integers); raises on error."""
     _check(lib().gsdr_lcs_decide_noalloc(d_packed, d_pack_off, d_len_raw, d_len_gf, n_seq,
                                          d_pat, d_txt, n_pairs, C.c_float(t), d_accept, stream))
+
+
+class Server:
+    """Continuous batching of clustering jobs on one GPU (gsdr_server_*)."""
+
+    def __init__(self, device=0, max_inflight=4, mem_budget=0, batch=0):
+        so = ServerOpts(device, max_inflight, mem_budget, batch)
+        h = C.c_void_p()
+        _check(lib().gsdr_server_create(C.byref(so), C.byref(h)))
+        self._h = h
+
+    def submit(self, fasta: bytes, threshold: float) -> int:
+        j = C.c_int64()
+        _check(lib().gsdr_server_submit(self._h, fasta, len(fasta), C.c_float(threshold),
+                                        C.byref(j)))
+        return j.value
+
+    def wait(self, timeout_ms=-1):
+        """Next finished job: (id, status, latency_ms), or None on timeout."""
+        j, st, lat = C.c_int64(), C.c_int32(), C.c_double()
+        rc = lib().gsdr_server_wait(self._h, timeout_ms, C.byref(j), C.byref(st), C.byref(lat))
+        if rc == ETIMEOUT:
+            return None
+        _check(rc)
+        return j.value, st.value, lat.value
+
+    def result(self, job):
+        """(representative FASTA bytes, cluster array) of a finished job."""
+        need, n = C.c_int64(), C.c_int32()
+        _check(lib().gsdr_server_result(self._h, job, None, 0, C.byref(need), None, C.byref(n)))
+        buf = C.create_string_buffer(max(need.value, 1))
+        cl = np.empty(max(n.value, 1), dtype=np.int32)
+        _check(lib().gsdr_server_result(self._h, job, buf, need.value, C.byref(need),
+                                        cl.ctypes.data, C.byref(n)))
+        return buf.raw[: need.value], cl[: n.value]
+
+    def release(self, job):
+        _check(lib().gsdr_server_release(self._h, job))
+
+    def close(self):
+        if self._h:
+            lib().gsdr_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def main(argv) -> int:
