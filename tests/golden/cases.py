@@ -1,0 +1,79 @@
+"""Inputs of the golden cases: every input is rebuilt byte for byte from
+these definitions (the synthetic generator and numpy's PCG64 are the same on
+every platform; the recorded input sha256 guards that)."""
+import gzip
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _edge_mixed(seed=9):
+    rng = np.random.default_rng(seed)
+    codes = np.frombuffer(b"ACGT", dtype=np.uint8)
+    base = codes[rng.integers(0, 4, 700)].tobytes()
+    recs = []
+    for i in range(60):
+        s = bytearray(base[: rng.integers(150, 700)])
+        for _ in range(rng.integers(0, 12)):
+            s[rng.integers(0, len(s))] = int(rng.choice(list(b"ACGTNRYacgtnu")))
+        if i % 7 == 0:
+            s += b"\r"
+        recs.append(b">r%d desc\n" % i + bytes(s) + b"\n")
+    recs.append(b">short1\nACG\n")
+    recs.append(b">short2\nACGTA\n")
+    recs.append(b">multiline\n" + base[:100] + b"\n" + base[100:300] + b"\n\n" + base[300:400] + b"\n")
+    recs.append(b">dup1\n" + base[:500] + b"\n")
+    recs.append(b">dup2\n" + base[:500] + b"\n")
+    return b"".join(recs)
+
+
+def _ties(seed=4):
+    rng = np.random.default_rng(seed)
+    codes = np.frombuffer(b"ACGT", dtype=np.uint8)
+    seeds = [codes[rng.integers(0, 4, 120)].tobytes() for _ in range(40)]
+    recs = []
+    for i in range(1500):
+        s = bytearray(seeds[i % 40])
+        for _ in range(rng.integers(0, 6)):
+            s[rng.integers(0, 120)] = int(codes[rng.integers(0, 4)])
+        recs.append(b">t%d\n" % i + bytes(s) + b"\n")
+    return b"".join(recs)
+
+
+def _reference_result():
+    with gzip.open(os.path.join(HERE, "ref_cuda_result.fasta.gz"), "rb") as f:
+        return f.read()
+
+
+# name: (input builder, cluster options as argv letters)
+CASES = {
+    "c0_10k_t95": (("synth", 0, 10000, None), ["t", "0.95"]),
+    "c0_3k_t90": (("synth", 0, 3000, 2), ["t", "0.90"]),
+    "c0_3k_t97": (("synth", 0, 3000, 3), ["t", "0.97"]),
+    "c0_2k_t88": (("synth", 0, 2000, 4), ["t", "0.88"]),
+    "c0_2k_w7": (("synth", 0, 2000, 5), ["t", "0.95", "w", "7"]),
+    "c0_800_t85_drop": (("synth", 0, 800, 6), ["t", "0.85"]),
+    "c0_800_t95_d1": (("synth", 0, 800, 7), ["t", "0.95", "d", "1"]),
+    "c1_20k_t95": (("synth", 1, 20000, 21), ["t", "0.95"]),
+    "c2_30k_t90": (("synth", 2, 30000, 31), ["t", "0.90"]),
+    "c4_3k_t90": (("synth", 4, 3000, 41), ["t", "0.90"]),
+    "ties_150bp_t95": (("fn", "ties"), ["t", "0.95"]),
+    "edge_mixed_t95": (("fn", "edge"), ["t", "0.95"]),
+    "edge_mixed_t90": (("fn", "edge"), ["t", "0.90"]),
+    "ref_result_t95": (("fn", "refres"), ["t", "0.95"]),
+}
+
+
+def build_input(spec):
+    if spec[0] == "synth":
+        import gsdr
+
+        _, cfg, n, seed = spec
+        kw = {}
+        if cfg == 4:
+            kw = dict(n_seeds=max(1, n // 5), len_lo=150, len_hi=5000)
+        return gsdr.synth_fasta(cfg, n_reads=n, seed=seed, **kw)
+    name = spec[1]
+    return {"ties": _ties, "edge": _edge_mixed, "refres": _reference_result}[name]()
