@@ -3,6 +3,7 @@
 // points, and gsdr_main (the CLI).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -64,7 +65,23 @@ struct Carve {
 struct Plan {
     std::vector<int64_t> pack_off, kmer_off;
     int64_t max_len = 0;
+    int r_max = 1;          // largest R (tentatives per pass)
+    int64_t idx_cap = 0;    // > 0: batched word filter by inverted index, postings capacity
+    bool idx_smem = false;  // that index fits the filter's shared memory (16-bit copy)
 };
+
+constexpr int kSmemOptin = 227 * 1024;  // per-block shared memory limit of sm_100 / sm_103
+
+// R_max of a job: the caller's batch, or 256 for the automatic choice.
+int job_r_max(const gsdr_opts& o) {
+    return o.batch == 0 ? 256 : (o.batch > kMaxBatch ? kMaxBatch : (o.batch < 1 ? 1 : o.batch));
+}
+
+// The batched word filter walks an inverted index of the tentatives' k-mers
+// when the reads hold few of the 4^k k-mers (mean distinct k-mers per read at
+// most 4^k / kIndexDensity): then almost every table lookup of the table form
+// would read a zero.  GSDR_BFILTER=index or =table forces either form.
+constexpr int64_t kIndexDensity = 8;
 
 int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
     const int n = reads->n;
@@ -72,18 +89,53 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
     const int k = o.word_length;
     P.pack_off.assign(n + 1, 0);
     P.kmer_off.assign(n + 1, 0);
+    P.r_max = o.batch == 1 ? 1 : job_r_max(o);
     const int64_t kcap = (int64_t)1 << (2 * (k > 0 ? k : 1));
+    int64_t ents_sum = 0, ents_max = 0;
+    std::vector<int64_t> head;  // entries of the first kMaxBatch reads, prefix sums
+    head.reserve(kMaxBatch + 1);
+    head.push_back(0);
+    bool sorted = true;
     for (int i = 0; i < n; i++) {
         const int64_t L = reads->length[i];
         if (L < 0) return fail(GSDR_EINVAL, "negative read length");
         if (reads->offset[i] < 0 || reads->offset[i] + L > reads->n_bytes)
             return fail(GSDR_EINVAL, "read outside the byte buffer");
         if (L > P.max_len) P.max_len = L;
+        if (i > 0 && L > reads->length[i - 1]) sorted = false;
         P.pack_off[i + 1] = P.pack_off[i] + round4(L / 16 + 1);
         int64_t ents = drop ? 0 : L - k + 1;
         if (ents < 0) ents = 0;
         if (ents > kcap) ents = kcap;
+        ents_sum += ents;
+        if (ents > ents_max) ents_max = ents;
+        if (i < kMaxBatch) head.push_back(head.back() + ents);
         P.kmer_off[i + 1] = P.kmer_off[i] + round4(ents);
+    }
+    if (o.batch != 1 && !drop && n > 0) {
+        bool index = ents_sum * kIndexDensity <= kcap * (int64_t)n;
+        const char* f = std::getenv("GSDR_BFILTER");
+        if (f && std::strcmp(f, "index") == 0) index = true;
+        if (f && std::strcmp(f, "table") == 0) index = false;
+        if (index) {
+            // a pass indexes at most R_max tentatives: for length-sorted reads
+            // those hold at most the first R_max reads' entries
+            auto cap_of = [&](int r) {
+                const int m = std::min<int>(r, (int)head.size() - 1);
+                return std::max<int64_t>(sorted ? head[m] : ents_max * r, 1);
+            };
+            if (o.batch == 0 && sorted) {
+                // automatic R: the largest R_max (in steps of 64, at least the
+                // default) whose index still fits the filter's shared memory
+                for (int r = kMaxBatch; r > P.r_max; r -= 64)
+                    if (index_in_smem(k, r, cap_of(r), kSmemOptin)) {
+                        P.r_max = r;
+                        break;
+                    }
+            }
+            P.idx_cap = cap_of(P.r_max);
+            P.idx_smem = index_in_smem(k, P.r_max, P.idx_cap, kSmemOptin);
+        }
     }
     return GSDR_OK;
 }
@@ -125,6 +177,13 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     B.survive = c.take<uint32_t>(kTTWords);
     B.acc_cap = 2 * B.seg_cap;
     B.acc = c.take<Pair>((size_t)B.acc_cap);
+    B.r_max = P.r_max;
+    B.idx_cap = P.idx_cap;
+    B.idx_off = P.idx_cap > 0 ? c.take<uint32_t>(((size_t)1 << (2 * k)) + 1) : nullptr;
+    B.idx_post = P.idx_cap > 0 ? c.take<uint32_t>((size_t)P.idx_cap) : nullptr;
+    // 16-byte copies read whole: both rounded up to 8 entries
+    B.idx_off16 = P.idx_smem ? c.take<uint16_t>(((size_t)1 << (2 * k)) + 8) : nullptr;
+    B.idx_post16 = P.idx_smem ? c.take<uint16_t>((size_t)P.idx_cap + 8) : nullptr;
     return c.used + 256;
 }
 
@@ -182,15 +241,13 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
         const char* tr = std::getenv("GSDR_TRACE");
         trace_ = tr && tr[0] == '1';
     }
-    r_max_ = opts.batch == 0 ? 256 : (opts.batch > kMaxBatch ? kMaxBatch : opts.batch);
-    stats.batch = batched_ ? r_max_ : 1;
     Plan P;
     rc = make_plan(reads, opts, P);
     if (rc) return rc;
+    r_max_ = P.r_max;
+    stats.batch = batched_ ? r_max_ : 1;
     if (P.max_len > 32 * kMaxPatternWords)
         return fail(GSDR_EUNSUPPORTED, "reads above 32768 bases are not built yet");
-    pack_off_.swap(P.pack_off);
-    kmer_off_.swap(P.kmer_off);
     int dev_count = 0;
     if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
         return fail(GSDR_EDEVICE, "no CUDA device");
@@ -206,13 +263,13 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     JCUDA(cudaMallocHost(&h_done_, sizeof(int32_t)));
     JCUDA(cudaMallocHost(&h_state_, sizeof(RoundState)));
     if (n == 0) return GSDR_OK;
-    Plan P2;
-    P2.pack_off = pack_off_;
-    P2.kmer_off = kmer_off_;
-    dbytes_ = carve_all(nullptr, n, n_bytes_, P2, opts.drop == 1, opts.word_length, R_, B_);
+    dbytes_ = carve_all(nullptr, n, n_bytes_, P, opts.drop == 1, opts.word_length, R_, B_);
     JCUDA(cudaMalloc(&dmem_, dbytes_));
-    carve_all(reinterpret_cast<char*>(dmem_), n, n_bytes_, P2, opts.drop == 1, opts.word_length,
+    carve_all(reinterpret_cast<char*>(dmem_), n, n_bytes_, P, opts.drop == 1, opts.word_length,
               R_, B_);
+    stats.word_index = P.idx_cap > 0 ? 1 : 0;
+    pack_off_.swap(P.pack_off);
+    kmer_off_.swap(P.kmer_off);
     return GSDR_OK;
 }
 
@@ -345,6 +402,7 @@ int Job::run() {
     JCUDA(cudaStreamSynchronize(stream));
     JCUDA(cudaGetLastError());
     if (h_state_->error == 2) return fail(GSDR_ENOMEM, "alignment queue overflow");
+    if (h_state_->error == 3) return fail(GSDR_EDEVICE, "k-mer index capacity exceeded");
     if (h_state_->error) return fail(GSDR_ETIMEOUT, "a device-side wait gave up");
     if (!batched_ && h_state_->pair_overflow) return fail(GSDR_EDEVICE, "alignment queue overflow");
     float ms = 0;

@@ -110,6 +110,16 @@ struct RoundBuffers {
     uint32_t* survive;   // kTTWords
     Pair* acc;           // accepted pairs of the pass
     int32_t acc_cap;
+    // batched word filter by inverted index (sparse k-mer spaces; null = the
+    // per-tentative table form): for k-mer m, idx_post[idx_off[m] ..
+    // idx_off[m + 1]) holds (tentative << 16 | count) of every tentative with
+    // a non-zero count of m.  Rebuilt every pass.
+    uint32_t* idx_off;   // 4^k + 1
+    uint32_t* idx_post;  // idx_cap
+    uint16_t* idx_off16;   // 16-bit copies for the shared-memory form (null otherwise)
+    uint16_t* idx_post16;
+    int64_t idx_cap;
+    int32_t r_max;       // largest R of the job (sizes the index filter's shared memory)
 };
 void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s);
 // One plain round (filter, align, compact, advance); `parity` picks which
@@ -122,6 +132,7 @@ void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity
 void launch_align_stage(const DevReads& R, RoundBuffers& B, bool batched_mapping, bool greedy,
                         cudaStream_t s);
 int align_class_host(int words);
+bool index_in_smem(int k, int r_max, int64_t cap, int smem_optin);
 // One batched pass (select, filter, align, resolve, compact, advance).
 void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,
                        long long* count, cudaEvent_t* ev4);

@@ -653,6 +653,300 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundSta
     }
 }
 
+// ---- word filter by inverted index (sparse k-mer spaces) -------------------
+//
+// With short reads and k = 7 a tentative holds ~1% of the 4^k k-mers, so the
+// table form spends almost every lookup on a zero.  Instead, each pass lists,
+// per k-mer, the tentatives that hold it (k_bindex), and every candidate walks
+// the lists of its own k-mers once, adding min(count in tentative, count in
+// candidate) into one 16-bit counter per tentative (k_bfilter_idx).  The sums
+// are the same integers kernel_filter forms (func.cu:803-826); only the order
+// of the additions differs.
+
+constexpr int kIndexThreads = 1024;
+
+// One CTA: histogram of the tentatives' k-mers, exclusive scan into idx_off,
+// scatter of (tentative << 16 | count) into idx_post.  The order inside one
+// k-mer's list is arbitrary; the filter's sums do not depend on it.  With
+// off16/post16 (capacity below 65536) it also writes the 16-bit copy that
+// k_bfilter_idx keeps in shared memory: (tentative << 6 | min(count, 63)).
+template <int K>
+__global__ void __launch_bounds__(kIndexThreads, 1) k_bindex(DevReads R, RoundState* st,
+                                                          const int32_t* __restrict__ tent,
+                                                          uint32_t* idx_off, uint32_t* idx_post,
+                                                          uint16_t* off16, uint16_t* post16,
+                                                          long long idx_cap) {
+    constexpr int NB = 1 << (2 * K);
+    constexpr int PER = NB >= kIndexThreads ? NB / kIndexThreads : 1;
+    extern __shared__ uint32_t cnt[];  // NB counters, then the scatter cursors
+    __shared__ uint32_t wsum[32];
+    if (st->done || st->n_tent == 0) return;
+    const int nt = st->n_tent;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < NB; i += kIndexThreads) cnt[i] = 0u;
+    __syncthreads();
+    for (int t = warp; t < nt; t += kIndexThreads / 32) {
+        const int rep = tent[t];
+        const uint32_t* e = R.kmer + R.kmer_off[rep];
+        const int ne = R.n_kmer[rep];
+        for (int i = lane; i < ne; i += 32) {
+            const uint32_t v = __ldg(e + i);
+            if (v & 0xffffu) atomicAdd(&cnt[v >> 16], 1u);
+        }
+    }
+    __syncthreads();
+    // exclusive scan: thread i owns counters [i*PER, i*PER + PER)
+    const int base = threadIdx.x * PER;
+    uint32_t run = 0;
+#pragma unroll
+    for (int j = 0; j < PER; j++) run += base + j < NB ? cnt[base + j] : 0u;
+    uint32_t incl = run;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t o = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += o;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < kIndexThreads / 32; w++) {
+        const uint32_t s = wsum[w];
+        if (w < warp) before += s;
+        total += s;
+    }
+    uint32_t pos = before + incl - run;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+        if (base + j < NB) {
+            const uint32_t c = cnt[base + j];
+            idx_off[base + j] = pos;
+            if (off16) off16[base + j] = (uint16_t)pos;
+            cnt[base + j] = pos;  // becomes the scatter cursor
+            pos += c;
+        }
+    }
+    if (threadIdx.x == 0) {
+        idx_off[NB] = total;
+        if (off16) off16[NB] = (uint16_t)total;
+    }
+    if ((long long)total > idx_cap) {
+        // cannot happen for length-sorted reads (the capacity holds the R_max
+        // longest k-mer lists); stop the job instead of writing past the end
+        if (threadIdx.x == 0) {
+            st->error = 3;
+            st->done = 1;
+        }
+        return;
+    }
+    __syncthreads();
+    for (int t = warp; t < nt; t += kIndexThreads / 32) {
+        const int rep = tent[t];
+        const uint32_t* e = R.kmer + R.kmer_off[rep];
+        const int ne = R.n_kmer[rep];
+        for (int i = lane; i < ne; i += 32) {
+            const uint32_t v = __ldg(e + i);
+            const uint32_t c = v & 0xffffu;
+            if (c) {
+                const uint32_t at = atomicAdd(&cnt[v >> 16], 1u);
+                idx_post[at] = ((uint32_t)t << 16) | c;
+                if (post16) post16[at] = (uint16_t)(((uint32_t)t << 6) | min(c, 63u));
+            }
+        }
+    }
+}
+
+// Shared memory of k_bfilter_idx, in 32-bit words, every region on a 16-byte
+// boundary.  SMEM form: the whole index as 16-bit entries (offsets, and
+// postings (tentative << 6 | min(count, 63)), 63 meaning "read the exact count
+// from the 32-bit list"); otherwise the 32-bit offsets only.  Then the
+// tentatives, and per warp the 16-bit sums (two per word).
+constexpr int kIdxGroups = 8;  // groups of 32 k-mer entries held in registers at a time
+struct IndexSmem {
+    int off_words, post_words, tent_words, acc_words;
+    __host__ __device__ IndexSmem(int k, int r_max, long long cap, bool smem_index) {
+        const int nb1 = (1 << (2 * k)) + 1;
+        off_words = smem_index ? ((nb1 + 7) & ~7) / 2 : (nb1 + 3) & ~3;
+        post_words = smem_index ? (int)(((cap + 7) & ~7LL) / 2) : 0;
+        tent_words = (r_max + 3) & ~3;
+        acc_words = ((r_max + 1) / 2 + 3) & ~3;
+    }
+    __host__ __device__ int warp_words() const { return acc_words; }
+    __host__ __device__ int bytes(int warps) const {
+        return 4 * (off_words + post_words + tent_words + warps * warp_words());
+    }
+};
+
+template <int K, bool SMEM>
+__global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
+    DevReads R, RoundState* st, const int32_t* __restrict__ remain,
+    const int32_t* __restrict__ tent, const uint32_t* __restrict__ idx_off,
+    const uint32_t* __restrict__ idx_post, const uint16_t* __restrict__ off16,
+    const uint16_t* __restrict__ post16, int r_max, long long cap, Pair* pairs, int seg_cap) {
+    constexpr int NB = 1 << (2 * K);
+    extern __shared__ __align__(16) uint32_t sm[];
+    if (st->done || st->n_tent == 0) return;
+    const IndexSmem L(K, r_max, cap, SMEM);
+    const int warps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint16_t* s_off16 = reinterpret_cast<uint16_t*>(sm);
+    uint32_t* s_off32 = sm;
+    uint16_t* s_post16 = reinterpret_cast<uint16_t*>(sm + L.off_words);
+    int32_t* s_tent = reinterpret_cast<int32_t*>(sm + L.off_words + L.post_words);
+    uint32_t* const acc = sm + L.off_words + L.post_words + L.tent_words + warp * L.warp_words();
+    const int nt = st->n_tent;
+    const int n = st->n_remain;
+    if (SMEM) {
+        const int total = (int)idx_off[NB];
+        const uint4* g = reinterpret_cast<const uint4*>(post16);
+        uint4* d = reinterpret_cast<uint4*>(s_post16);
+        for (int i = threadIdx.x; i < (total + 7) >> 3; i += blockDim.x) d[i] = __ldg(g + i);
+        const uint4* go = reinterpret_cast<const uint4*>(off16);
+        uint4* dof = reinterpret_cast<uint4*>(s_off16);
+        for (int i = threadIdx.x; i < (NB + 1 + 7) >> 3; i += blockDim.x) dof[i] = __ldg(go + i);
+    } else {
+        for (int i = threadIdx.x; i < NB + 1; i += blockDim.x) s_off32[i] = __ldg(idx_off + i);
+    }
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) s_tent[i] = tent[i];
+    for (int i = lane; i < L.acc_words; i += 32) acc[i] = 0u;
+    __syncthreads();
+    unsigned long long n_pf = 0, bytes = 0;
+    unsigned n_wf = 0, n_al = 0;
+    const int nwarps = gridDim.x * warps;
+    // software pipeline over the warp's candidates: the next candidate's read
+    // index and k-mer list position load while this one is summed
+    int idx = blockIdx.x * warps + warp;
+    int q_nx = idx < n ? remain[idx] : 0;
+    const uint32_t* e_nx = R.kmer + (idx < n ? R.kmer_off[q_nx] : 0);
+    int ne_nx = idx < n ? R.n_kmer[q_nx] : 0;
+    for (; idx < n; idx += nwarps) {
+        const int q = q_nx;
+        const uint32_t* const e = e_nx;
+        const int ne = ne_nx;
+        if (idx + nwarps < n) q_nx = remain[idx + nwarps];
+        // tentatives before q: the first ntq of the ascending list (all of
+        // them for every candidate past the last tentative)
+        int lo = 0, hi = nt;
+        if (s_tent[nt - 1] < q) lo = nt;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (s_tent[mid] < q) lo = mid + 1;
+            else hi = mid;
+        }
+        const int ntq = lo;
+        if (ntq > 0) {
+            n_pf += ntq;
+            bytes += 4ull * (unsigned)ne;
+        }
+        // sum over q's k-mers of min(count in q, count in tentative), per
+        // tentative.  The warp takes 32 k-mers at a time, one per lane, and
+        // lays their tentative lists end to end (a prefix sum of the list
+        // lengths); then every lane takes one position of that concatenation
+        // per step and finds the k-mer it belongs to by binary search over the
+        // lanes' start positions, so no lane idles while another list is long.
+        // Up to kIdxGroups groups of 32 entries load at once.
+        for (int c0 = 0; c0 < (ntq > 0 ? ne : 0); c0 += 32 * kIdxGroups) {
+            uint32_t vg[kIdxGroups];
+#pragma unroll
+            for (int g = 0; g < kIdxGroups; g++) {
+                const int i = c0 + 32 * g + lane;
+                vg[g] = i < ne ? __ldcs(e + i) : 0u;
+            }
+            if (c0 == 0 && idx + nwarps < n) {
+                // the next candidate's list position (its index arrived by now)
+                e_nx = R.kmer + R.kmer_off[q_nx];
+                ne_nx = R.n_kmer[q_nx];
+            }
+#pragma unroll
+            for (int g = 0; g < kIdxGroups; g++) {
+                if (c0 + 32 * g >= ne) break;
+                const uint32_t v = vg[g];
+                const uint32_t km = v >> 16;
+                const uint32_t c = v & 0xffffu;
+                const uint32_t s0 = SMEM ? s_off16[km] : s_off32[km];
+                const uint32_t sz = c ? (SMEM ? s_off16[km + 1] : s_off32[km + 1]) - s0 : 0u;
+                uint32_t incl = sz;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t o = __shfl_up_sync(kFull, incl, d);
+                    if (lane >= d) incl += o;
+                }
+                const uint32_t excl = incl - sz;
+                const uint32_t total = __shfl_sync(kFull, incl, 31);
+                const uint32_t jbase = s0 - excl;  // posting index = jbase + position
+                for (uint32_t base = 0; base < total; base += 32) {
+                    const uint32_t p = base + lane;
+                    // the last lane whose list starts at or before p owns p
+                    int o = 0;
+#pragma unroll
+                    for (int step = 16; step >= 1; step >>= 1) {
+                        const uint32_t x = __shfl_sync(kFull, excl, o + step);
+                        if (x <= p) o += step;
+                    }
+                    const uint32_t j = __shfl_sync(kFull, jbase, o) + p;
+                    const uint32_t co = __shfl_sync(kFull, c, o);
+                    if (p < total) {
+                        uint32_t t, ct;
+                        if (SMEM) {
+                            const uint32_t pp = s_post16[j];
+                            t = pp >> 6;
+                            ct = pp & 63u;
+                            if (ct == 63u) ct = __ldg(idx_post + j) & 0xffffu;
+                        } else {
+                            const uint32_t pp = __ldg(idx_post + j);
+                            t = pp >> 16;
+                            ct = pp & 0xffffu;
+                        }
+                        // 16-bit halves cannot carry: a sum is at most the
+                        // candidate's k-mer count, below 32768
+                        if (t < (uint32_t)ntq)
+                            atomicAdd(&acc[t >> 1], min(ct, co) << ((t & 1u) << 4));
+                    }
+                }
+            }
+        }
+        if (!(ntq > 0 && ne > 0) && idx + nwarps < n) {
+            e_nx = R.kmer + R.kmer_off[q_nx];
+            ne_nx = R.n_kmer[q_nx];
+        }
+        if (ntq == 0) continue;
+        __syncwarp();
+        // the tentatives whose sum reaches the cutoff pass the word filter;
+        // the composition bound (kernel_preFilter, func.cu:738-754) decides
+        // the rest.  The sums are cleared on the way.
+        const int cw = R.cut_word[q];
+        uint4* a4 = reinterpret_cast<uint4*>(acc);
+        const int w4 = (ntq + 7) >> 3;
+        for (int i = lane; i < w4; i += 32) {
+            const uint4 a = a4[i];
+            a4[i] = make_uint4(0u, 0u, 0u, 0u);
+            const uint32_t w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+            for (int h = 0; h < 8; h++) {
+                const int t = 8 * i + h;
+                const int s = (int)((w[h >> 1] >> ((h & 1) << 4)) & 0xffffu);
+                if (t < ntq && !(s < cw)) {
+                    n_wf++;
+                    const int rep = s_tent[t];
+                    if (prefilter_pass(R.comp[rep], R.comp[q], R.cut_base[q])) {
+                        push_pair(st, pairs, seg_cap, R, rep, q);
+                        n_al++;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+    // n_pf and bytes are the same in every lane; n_wf and n_al are per lane
+    n_wf = (unsigned)warp_sum_i((int)n_wf);
+    n_al = (unsigned)warp_sum_i((int)n_al);
+    if (lane == 0) {
+        if (n_pf) atomicAdd(&st->cnt_prefilter, n_pf);
+        if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
+        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
+        if (bytes) atomicAdd(&st->filter_bytes, bytes);
+    }
+}
+
 // Survival of the tentatives in greedy order (one warp): a tentative survives
 // iff no surviving earlier tentative accepted it.  Only rows with a bit can
 // claim anything, so only those are visited, in increasing order.
@@ -828,9 +1122,54 @@ void launch_bfilter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
                                                           B.seg_cap);
 }
 
+template <int K>
+void launch_bfilter_idx_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
+                          cudaStream_t s) {
+    const bool in_smem = B.idx_post16 != nullptr;
+    const int threads = in_smem ? 1024 : 256;
+    const int ismem = (1 << (2 * K)) * 4;
+    const int fsmem = IndexSmem(K, B.r_max, B.idx_cap, in_smem).bytes(threads / 32);
+    static bool attr = false;
+    if (!attr) {
+        // the device's largest size, set once: jobs of one process may run
+        // concurrently with different index sizes
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncSetAttribute(k_bindex<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, ismem);
+        cudaFuncSetAttribute(k_bfilter_idx<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin);
+        cudaFuncSetAttribute(k_bfilter_idx<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin);
+        attr = true;
+    }
+    k_bindex<K><<<1, kIndexThreads, ismem, s>>>(R, B.st, B.tent, B.idx_off, B.idx_post,
+                                                B.idx_off16, B.idx_post16, (long long)B.idx_cap);
+    if (in_smem) {
+        const int grid = grid_for(k_bfilter_idx<K, true>, threads, fsmem, 2);
+        k_bfilter_idx<K, true><<<grid, threads, fsmem, s>>>(
+            R, B.st, remain, B.tent, B.idx_off, B.idx_post, B.idx_off16, B.idx_post16, B.r_max,
+            (long long)B.idx_cap, B.pairs, B.seg_cap);
+    } else {
+        const int grid = grid_for(k_bfilter_idx<K, false>, threads, fsmem, 8);
+        k_bfilter_idx<K, false><<<grid, threads, fsmem, s>>>(
+            R, B.st, remain, B.tent, B.idx_off, B.idx_post, nullptr, nullptr, B.r_max,
+            (long long)B.idx_cap, B.pairs, B.seg_cap);
+    }
+}
+
 template <bool BATCH>
 void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain, int drop,
                        cudaStream_t s) {
+    if (BATCH && !drop && B.idx_off) {
+        switch (R.k) {
+            case 4: launch_bfilter_idx_t<4>(R, B, remain, s); break;
+            case 5: launch_bfilter_idx_t<5>(R, B, remain, s); break;
+            case 6: launch_bfilter_idx_t<6>(R, B, remain, s); break;
+            default: launch_bfilter_idx_t<7>(R, B, remain, s); break;
+        }
+        return;
+    }
     if (drop) {
         if (BATCH) launch_bfilter_t<4, true>(R, B, remain, s);
         else launch_filter_t<4, true>(R, B, remain, s);
@@ -954,7 +1293,15 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 8 + kAlignClasses - 3;
+    if (count) *count += 8 + kAlignClasses - 3 + (!drop && B.idx_off ? 1 : 0);
+}
+
+// Whether a job's per-pass k-mer index (at most `cap` postings) is kept in
+// shared memory by the index filter: 16-bit offsets need cap < 65536, and the
+// layout for a 1024-thread CTA must fit the device's per-block maximum.
+bool index_in_smem(int k, int r_max, int64_t cap, int smem_optin) {
+    if (cap <= 0 || cap >= 65536) return false;
+    return IndexSmem(k, r_max, cap, true).bytes(1024 / 32) <= smem_optin;
 }
 
 }  // namespace gsdr

@@ -74,6 +74,7 @@ class Stats(C.Structure):
         ("pigeon", C.c_int32),
         ("batch", C.c_int32),
         ("kernel_launches", C.c_int64),
+        ("word_index", C.c_int32),
     ]
 
     def as_dict(self):

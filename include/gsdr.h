@@ -66,7 +66,8 @@ typedef struct {
     int64_t rounds;           /* representatives taken (one per round in the plain form) */
     int64_t passes;           /* device passes (batched: one per batch of tentatives) */
     int64_t pairs_prefilter;  /* (representative, candidate) pairs that reached the prefilter */
-    int64_t pairs_word;       /* pairs that reached the word filter */
+    int64_t pairs_word;       /* pairs that reached the word filter (word_index = 1: pairs
+                                 that passed it; that form applies the word filter first) */
     int64_t pairs_aligned;    /* pairs that reached the alignment */
     int64_t pairs_accepted;
     double cells;             /* sum over aligned pairs of gap-free q x T (full-DP cells) */
@@ -75,6 +76,8 @@ typedef struct {
     double ms_filter, ms_align; /* with stage_timing only */
     int32_t k, drop, pigeon, batch;
     int64_t kernel_launches;  /* kernels launched by the library during the call */
+    int32_t word_index;       /* 1: the batched word filter used the per-pass inverted
+                                 k-mer index (reads holding few of the 4^k k-mers) */
 } gsdr_stats;
 
 /* Fill `o` with the reference defaults (t 0.95, derived k/drop, pigeon 0). */

@@ -1,0 +1,99 @@
+"""Batched word filter by per-pass inverted k-mer index (chosen automatically
+for reads holding few of the 4^k k-mers, e.g. 150 bp reads at k = 7) against
+the oracle: identical cluster arrays and FASTA bytes, in both filter forms, at
+every R, every word length, and for reads too short to hold a k-mer (the
+reference's kernel_filter, cuda-version/func.cu:803-826)."""
+import numpy as np
+import pytest
+
+import gsdr
+import oracle_binding as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def run_form(data, tmp_path, monkeypatch, t, batch, form, w=0, d=3):
+    if form is None:
+        monkeypatch.delenv("GSDR_BFILTER", raising=False)
+    else:
+        monkeypatch.setenv("GSDR_BFILTER", form)
+    _, ocl, ost, ofa = orc.run_bytes(data, tmp_path, t=t, w=w, d=d)
+    f = gsdr.Fasta.parse(data)
+    opts = gsdr.default_opts(threshold=t, drop=d, batch=batch, word_length=w)
+    cl, st = gsdr.clustering(f, opts, stats=True)
+    out = f.format(cl)
+    f.close()
+    bad = np.nonzero(cl != ocl)[0]
+    assert len(bad) == 0, f"{form} R={batch}: {len(bad)} reads differ, first {bad[:8]}"
+    assert out == ofa
+    assert st.rounds == ost.rounds
+    assert st.pairs_accepted == ost.accepted
+    return st, ost
+
+
+@pytest.mark.parametrize("batch", [2, 64, 256, 1024, 0])
+def test_c2_recipe_index_auto(tmp_path, monkeypatch, batch):
+    data = gsdr.synth_fasta(2, n_reads=30000, seed=33)
+    st, ost = run_form(data, tmp_path, monkeypatch, 0.90, batch, None)
+    assert st.k == 7 and st.word_index == 1
+    # the pairs sent to the alignment are the pairs passing both filters
+    assert st.passes < st.rounds
+
+
+def test_c2_recipe_same_pairs_both_forms(tmp_path, monkeypatch):
+    data = gsdr.synth_fasta(2, n_reads=20000, seed=34)
+    si, _ = run_form(data, tmp_path, monkeypatch, 0.90, 128, "index")
+    stt, _ = run_form(data, tmp_path, monkeypatch, 0.90, 128, "table")
+    assert si.word_index == 1 and stt.word_index == 0
+    assert si.pairs_prefilter == stt.pairs_prefilter
+    assert si.pairs_aligned == stt.pairs_aligned
+    assert si.cells == stt.cells
+
+
+@pytest.mark.parametrize("t", [0.88, 0.90, 0.93, 0.97])
+def test_index_forced_word_lengths(tmp_path, monkeypatch, t):
+    data = gsdr.synth_fasta(0, n_reads=2000, seed=35)
+    st, ost = run_form(data, tmp_path, monkeypatch, t, 64, "index")
+    assert st.word_index == 1 and st.k == ost.k
+
+
+@pytest.mark.parametrize("w", [4, 5, 6, 7])
+def test_index_forced_word_override(tmp_path, monkeypatch, w):
+    data = gsdr.synth_fasta(0, n_reads=1500, seed=36)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 32, "index", w=w)
+    assert st.k == w and st.word_index == 1
+
+
+def test_index_long_reads(tmp_path, monkeypatch):
+    data = gsdr.synth_fasta(1, n_reads=5000, seed=37)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 256, "index")
+    assert st.word_index == 1
+
+
+@pytest.mark.parametrize("form", ["index", "table"])
+def test_very_short_reads(tmp_path, monkeypatch, form):
+    # 3-48 bp reads at k = 7: reads of at most 6 bases hold no k-mer, and the
+    # word cutoff is never below 1 (func.cu:312-337), so they are never aligned
+    data = gsdr.synth_fasta(0, n_reads=3000, seed=38, len_lo=3, len_hi=40, n_seeds=400)
+    lens = np.array([len(l) for l in data.split(b"\n")[1::2]])
+    cw, _, _ = orc.cutoffs(lens, 0.90, 7)
+    assert (lens <= 6).any() and (cw >= 1).all()
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.90, 64, form, w=7)
+    assert st.word_index == (1 if form == "index" else 0)
+
+
+def test_index_form_is_repeatable(monkeypatch):
+    monkeypatch.setenv("GSDR_BFILTER", "index")
+    data = gsdr.synth_fasta(2, n_reads=20000, seed=39)
+    f = gsdr.Fasta.parse(data)
+    opts = gsdr.default_opts(threshold=0.90, batch=0)
+    job = gsdr.Job(f, opts)
+    try:
+        assert job.run().word_index == 1
+        a = job.cluster()
+        job.run()
+        b = job.cluster()
+    finally:
+        job.close()
+        f.close()
+    assert np.array_equal(a, b)
