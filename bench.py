@@ -111,6 +111,58 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def key_figures():
+    """`name: value` lines of profiles/key_figures.txt (figures read from ncu
+    captures; the commands are in the per-kernel summaries beside it)."""
+    out = {}
+    try:
+        with open(os.path.join(ROOT, "profiles", "key_figures.txt")) as fh:
+            for ln in fh:
+                ln = ln.split("#", 1)[0].strip()
+                if ":" in ln:
+                    k, v = ln.split(":", 1)
+                    v = v.strip()
+                    try:
+                        out[k.strip()] = float(v)
+                    except ValueError:
+                        out[k.strip()] = v
+    except OSError:
+        pass
+    return out
+
+
+def filter_roofline(r, figures):
+    """The filter stage against HBM: algorithmic bytes (each candidate's
+    (k-mer, count) list once per launch) over the stage's event-timed launch
+    durations; traffic = the ncu DRAM bytes per algorithmic byte of the same
+    kernel scaled to this run's bytes per launch."""
+    launches = max(1, r["filter_launches"])
+    per_launch = r["filter_bytes"] / launches
+    achieved = r["filter_gbs"]
+    key = "filter_index" if r["word_index"] else "filter_table"
+    ratio = figures.get("%s.dram_over_algorithmic" % key)
+    return {"bound": "hbm",
+            "kernel": "k_bfilter_idx (inverted k-mer index)" if r["word_index"]
+            else "k_bfilter / k_filter (k-mer tables)",
+            "achieved": achieved, "peak": r["peak"], "unit": "GB/s",
+            "frac": achieved / r["peak"] if r["peak"] else None,
+            "peak_source": r["peak_kind"] + " (MEASURED_PEAKS.json hbm_gbs)"
+            if r["peak_kind"] == "measured" else r["peak_kind"],
+            "traffic": per_launch * ratio if isinstance(ratio, float) else None,
+            "algorithmic_bytes_per_launch": per_launch, "launches": launches,
+            "stage_ms": r["filter_ms"]}
+
+
+def align_roofline(r, figures):
+    """The alignment stage is integer-ALU bound (bit-parallel LCS): GCUPS over
+    the full-DP cells of the pairs it decides, and the ALU pipe utilisation
+    ncu measured for its dominant kernel."""
+    return {"bound": "int_alu", "kernel": "k_align_single / k_align",
+            "gcups": r["gcups"], "stage_ms": r["align_ms"], "cells": r["stats"]["cells"],
+            "alu_pipe_pct_ncu": figures.get("align.alu_pipe_pct"),
+            "ipc_ncu": figures.get("align.ipc")}
+
+
 def oracle_lib():
     import oracle_binding
 
@@ -209,6 +261,20 @@ def bench_ours(args, rank, world, local):
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     same = bool((cl == cl_dev).all())
 
+    # the plain form (one representative per round, the reference's loop) on
+    # the same device-resident reads: the batched / plain ratio
+    plain = None
+    if args.batch != 1 and args.plain_steps > 0:
+        pj = gsdr.Job(f, gsdr.default_opts(threshold=t, device=device, batch=1))
+        pj.run()
+        pms = []
+        for _ in range(args.plain_steps):
+            s = pj.run()
+            pms.append(s.ms_prep + s.ms_cluster)
+        plain = {"ms": sum(pms) / len(pms), "steps": len(pms),
+                 "same": bool((pj.cluster() == cl_dev).all())}
+        pj.close()
+
     # stage-timed run for the roofline (events around each filter / align launch)
     st_t = gsdr.clustering(f, gsdr.default_opts(threshold=t, device=device, batch=args.batch,
                                                 stage_timing=1), stats=True)[1]
@@ -225,8 +291,9 @@ def bench_ours(args, rank, world, local):
         "h2d": h2d, "d2h": d2h, "launches_per_step": launches // max(1, args.steps),
         "stats": last.as_dict(), "clocks": clock_info, "same": same,
         "filter_gbs": filt_gbs, "filter_ms": st_t.ms_filter, "filter_bytes": st_t.filter_bytes,
-        "filter_launches": st_t.rounds, "align_ms": st_t.ms_align, "gcups": align_gcups,
-        "peak": peak, "peak_kind": peak_kind, "t": t,
+        "filter_launches": st_t.passes if args.batch != 1 else st_t.rounds, "align_ms": st_t.ms_align, "gcups": align_gcups,
+        "peak": peak, "peak_kind": peak_kind, "t": t, "plain": plain,
+        "word_index": st_t.word_index, "r_max": st_t.batch,
     }
 
 
@@ -241,7 +308,12 @@ def main():
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--batch", type=int, default=0, help="0 = batched, adaptive R up to 256; 1 = plain")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--plain-steps", type=int, default=None,
+                    help="timed runs of the plain form for the batched/plain ratio "
+                         "(default 2 for the 10k and 200k workloads, else 0)")
     args = ap.parse_args()
+    if args.plain_steps is None:
+        args.plain_steps = 2 if args.config in (0, 1) else 0
     rank, world, local = dist_env()
 
     if world > 1:
@@ -274,6 +346,13 @@ def main():
     n_total = r["n"] * world
     value = n_total / (r["ms_step"] * 1e-3)
     e2e = n_total / (r["e2e_ms"] * 1e-3)
+    figures = key_figures()
+    plain_line = None
+    if r["plain"]:
+        pv = n_total / (r["plain"]["ms"] * 1e-3)
+        plain_line = {"value": pv, "unit": "seqs/s", "ms_per_step": r["plain"]["ms"],
+                      "steps": r["plain"]["steps"], "batched_over_plain": value / pv,
+                      "same_clusters": r["plain"]["same"]}
     line = {
         "metric": "seqs/sec", "value": value, "unit": "seqs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_step"],
@@ -287,16 +366,13 @@ def main():
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
         "gpu_launches": r["launches_per_step"] * args.steps,
         "clocks": r["clocks"],
-        "roofline": {"bound": "hbm", "kernel": "k_filter (prefilter + word filter)",
-                     "achieved": r["filter_gbs"], "peak": r["peak"], "unit": "GB/s",
-                     "frac": r["filter_gbs"] / r["peak"] if r["peak"] else None,
-                     "peak_source": r["peak_kind"], "traffic": None,
-                     "stage_ms": r["filter_ms"], "bytes": r["filter_bytes"]},
-        "align": {"gcups": r["gcups"], "stage_ms": r["align_ms"],
-                  "cells": r["stats"]["cells"]},
+        "roofline": filter_roofline(r, figures),
+        "align_roofline": align_roofline(r, figures),
+        "dominant_kernel": figures.get("c%d.dominant_kernel" % args.config),
+        "plain": plain_line,
         "stats": {k: r["stats"][k] for k in ("rounds", "passes", "pairs_prefilter", "pairs_word",
                                                "pairs_aligned", "pairs_accepted", "ms_prep",
-                                               "ms_cluster")},
+                                               "ms_cluster", "word_index", "batch")},
         "device_result_matches_e2e": r["same"],
     }
     if not args.no_cpu:

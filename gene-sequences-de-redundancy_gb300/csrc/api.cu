@@ -17,6 +17,7 @@
 #include "gsdr_host.h"
 #include "gsdr_testing.h"
 #include "job.h"
+#include "lcs_band.cuh"
 
 namespace gsdr {
 
@@ -356,9 +357,13 @@ int Job::loop_timed() {
             if (cudaMemcpy(&h, B_.st, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess)
                 std::fprintf(stderr,
                              "gsdr trace: step %lld rounds %lld tentatives %d R %d remain %d "
-                             "aligned %llu filter %.3f ms align %.3f ms\n",
+                             "aligned %llu filter %.3f ms align %.3f ms filter_bytes %llu "
+                             "queues %d %d %d %d %d %d | %d %d %d %d\n",
                              (long long)h.passes, (long long)h.rounds, h.n_tent, h.R, h.n_remain,
-                             (unsigned long long)h.cnt_aligned, a, b);
+                             (unsigned long long)h.cnt_aligned, a, b,
+                             (unsigned long long)h.filter_bytes, h.n_pairs[0], h.n_pairs[1],
+                             h.n_pairs[2], h.n_pairs[3], h.n_pairs[4], h.n_pairs[5], h.n_pairs[6],
+                             h.n_pairs[7], h.n_pairs[8], h.n_pairs[9]);
         }
         parity ^= 1;
         if (*h_done_) break;
@@ -569,13 +574,27 @@ int Job::lcs_pairs(const int32_t* pat, const int32_t* txt, int n_pairs, int mapp
     launch_pack(R_, opts.threshold, opts.word_length, stream);
     launch_planes(R_, stream);
     JCUDA(cudaGetLastError());
+    std::vector<int32_t> cut(n);
     JCUDA(cudaMemcpyAsync(gf.data(), R_.len_gf, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, stream));
+    JCUDA(cudaMemcpyAsync(cut.data(), R_.cut_base, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                          stream));
     JCUDA(cudaStreamSynchronize(stream));
     for (int k = 0; k < n_pairs; k++) {
         if (pat[k] < 0 || pat[k] >= n || txt[k] < 0 || txt[k] >= n || seen[pat[k]])
             return fail(GSDR_EINVAL, "lcs_pairs: bad or repeated pattern index");
         seen[pat[k]] = 1;
-        cls[align_class_host((gf[pat[k]] + 31) >> 5)].push_back(Pair{txt[k], pat[k]});
+        int c = align_class_host((gf[pat[k]] + 31) >> 5);
+        if (mapping == 2) {
+            // the banded kernel where the band fits 32 words (as batched passes do)
+            const int T = gf[txt[k]], q = gf[pat[k]], cb = cut[pat[k]];
+            // (the serial-work limit of the passes is not applied: tests reach
+            // every window class with any length)
+            if (T > 0 && cb > 0 && q >= cb && T >= cb) {
+                const int bw = band_words(T, q, cb);
+                if (bw <= 32) c = kSysClasses + (bw <= 4 ? 0 : bw <= 8 ? 1 : bw <= 16 ? 2 : 3);
+            }
+        }
+        cls[c].push_back(Pair{txt[k], pat[k]});
     }
     RoundState st{};
     for (int c = 0; c < kAlignClasses; c++) {
@@ -593,7 +612,7 @@ int Job::lcs_pairs(const int32_t* pat, const int32_t* txt, int n_pairs, int mapp
     JCUDA(cudaMemsetAsync(B_.cluster, 0xff, sizeof(int32_t) * n, stream));
     JCUDA(cudaMemsetAsync(B_.tidx, 0xff, sizeof(uint32_t) * n, stream));
     JCUDA(cudaEventRecord(ev_[2], stream));
-    launch_align_stage(R_, B_, mapping == 1, greedy != 0, stream);
+    launch_align_stage(R_, B_, mapping >= 1, greedy != 0, stream);
     JCUDA(cudaGetLastError());
     JCUDA(cudaEventRecord(ev_[3], stream));
     JCUDA(cudaMemcpyAsync(h_state_, B_.st, sizeof(RoundState), cudaMemcpyDeviceToHost, stream));
@@ -601,7 +620,7 @@ int Job::lcs_pairs(const int32_t* pat, const int32_t* txt, int n_pairs, int mapp
     JCUDA(cudaMemcpyAsync(cl.data(), B_.cluster, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, stream));
     JCUDA(cudaStreamSynchronize(stream));
     if (h_state_->error) return fail(GSDR_ETIMEOUT, "lcs_pairs: a device-side wait gave up");
-    if (mapping == 1) {
+    if (mapping >= 1) {
         const int na = h_state_->n_acc;
         if (na > B_.acc_cap) return fail(GSDR_ENOMEM, "lcs_pairs: accept list overflow");
         std::vector<Pair> acc(na);

@@ -20,7 +20,10 @@
 namespace gsdr {
 
 constexpr int kMaxPatternWords = 1024;  // 8 warps x 32 lanes x 4 words: 32768 gap-free bases
-constexpr int kAlignClasses = 6;        // pattern length classes of the alignment kernels
+constexpr int kSysClasses = 6;          // pattern length classes of the systolic alignment kernels
+constexpr int kBandClasses = 4;         // window classes (4, 8, 16, 32 words) of the banded kernel
+constexpr int kAlignClasses = kSysClasses + kBandClasses;  // alignment queues
+constexpr int kSingleWorkSlot = 15;     // work counter of the merged single-warp systolic classes
 constexpr int kMaxBatch = 1024;         // tentative representatives per batched pass
 constexpr int kTTWords = kMaxBatch / 32;
 constexpr int kMaxBitsK = 6;            // k-mer presence bitmaps for k <= 6 (4^k bits per read)

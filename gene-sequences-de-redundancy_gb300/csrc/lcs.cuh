@@ -42,6 +42,79 @@ __device__ __forceinline__ void planes32(uint32_t u0, uint32_t u1, uint32_t& hi,
     lo = even_bits(b0 >> 1) | (even_bits(b1 >> 1) << 16);
 }
 
+// s[i] = v[i] + u[i] (+ carry) over 1, 2 or 4 words as one add-with-carry
+// chain; cy is the carry in and out (0 or 1).
+__device__ __forceinline__ void add1_carry(uint32_t& s0, uint32_t v0, uint32_t u0, uint32_t& cy) {
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "add.cc.u32 t, %1, 0xffffffff;\n\t"
+        "addc.cc.u32 %0, %2, %3;\n\t"
+        "addc.u32 %1, 0, 0;\n\t"
+        "}"
+        : "=r"(s0), "+r"(cy)
+        : "r"(v0), "r"(u0));
+}
+
+__device__ __forceinline__ void add2_carry(uint32_t& s0, uint32_t& s1, uint32_t v0, uint32_t v1,
+                                           uint32_t u0, uint32_t u1, uint32_t& cy) {
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "add.cc.u32 t, %2, 0xffffffff;\n\t"
+        "addc.cc.u32 %0, %3, %5;\n\t"
+        "addc.cc.u32 %1, %4, %6;\n\t"
+        "addc.u32 %2, 0, 0;\n\t"
+        "}"
+        : "=r"(s0), "=r"(s1), "+r"(cy)
+        : "r"(v0), "r"(v1), "r"(u0), "r"(u1));
+}
+
+__device__ __forceinline__ void add4_carry(uint32_t& s0, uint32_t& s1, uint32_t& s2, uint32_t& s3,
+                                           uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3,
+                                           uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3,
+                                           uint32_t& cy) {
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "add.cc.u32 t, %4, 0xffffffff;\n\t"
+        "addc.cc.u32 %0, %5, %9;\n\t"
+        "addc.cc.u32 %1, %6, %10;\n\t"
+        "addc.cc.u32 %2, %7, %11;\n\t"
+        "addc.cc.u32 %3, %8, %12;\n\t"
+        "addc.u32 %4, 0, 0;\n\t"
+        "}"
+        : "=r"(s0), "=r"(s1), "=r"(s2), "=r"(s3), "+r"(cy)
+        : "r"(v0), "r"(v1), "r"(v2), "r"(v3), "r"(u0), "r"(u1), "r"(u2), "r"(u3));
+}
+
+// One text base applied to W pattern words (Hyyro's LCS recurrence):
+//   M = match mask of the base (from the pattern's high / low bit planes H, Lo
+//   and the base's bits as full masks ch, cl), U = V & M & keep,
+//   V' = (V + U + cy) | (V & ~M), cy = carry out of the top word.
+// keep = 0 makes the step a no-op for a zero carry-in (U = 0, V' = V).
+template <int W>
+__device__ __forceinline__ void hyyro_step(uint32_t (&V)[W], const uint32_t (&H)[W],
+                                           const uint32_t (&Lo)[W], uint32_t ch, uint32_t cl,
+                                           uint32_t keep, uint32_t& cy) {
+    constexpr int C = W >= 4 ? 4 : W;
+#pragma unroll
+    for (int i = 0; i < W; i += C) {
+        uint32_t m[C], u[C], s[C];
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            m[j] = ~((H[i + j] ^ ch) | (Lo[i + j] ^ cl));
+            u[j] = V[i + j] & m[j] & keep;
+        }
+        if constexpr (C == 4)
+            add4_carry(s[0], s[1], s[2], s[3], V[i], V[i + 1], V[i + 2], V[i + 3], u[0], u[1],
+                       u[2], u[3], cy);
+        else if constexpr (C == 2)
+            add2_carry(s[0], s[1], V[i], V[i + 1], u[0], u[1], cy);
+        else
+            add1_carry(s[0], V[i], u[0], cy);
+#pragma unroll
+        for (int j = 0; j < C; j++) V[i + j] = s[j] | (V[i + j] & ~m[j]);
+    }
+}
+
 __device__ __forceinline__ int warp_sum_i(int v) {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);

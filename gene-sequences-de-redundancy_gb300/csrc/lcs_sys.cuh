@@ -123,14 +123,7 @@ __device__ __forceinline__ void sys_steps8(const uint32_t* __restrict__ rb,
         if (MULTI) cin = not_lane0 ? from : ((cin8 >> j) & 1u);
         const uint32_t b = rb[j];
         const uint32_t ch = sign_mask<0>(b), cl = sign_mask<1>(b), inv = sign_mask<2>(b);
-#pragma unroll
-        for (int i = 0; i < W; i++) {
-            const uint32_t m = ~((H[i] ^ ch) | (Lo[i] ^ cl));
-            const uint32_t u = V[i] & m & ~inv;
-            const uint64_t t = (uint64_t)V[i] + u + cin;
-            cin = (uint32_t)(t >> 32);
-            V[i] = (uint32_t)t | (V[i] & ~m);
-        }
+        hyyro_step<W>(V, H, Lo, ch, cl, ~inv, cin);
         if (MULTI) out8 |= cin << j;
         // lane 0 receives its own carry-out from the shuffle: a single warp
         // clears it (its lane-0 carry-in is zero); a group member ignores it

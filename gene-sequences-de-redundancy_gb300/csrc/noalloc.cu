@@ -35,8 +35,8 @@ constexpr int kNaMaxDevices = 64;
 
 // Layout of the array (offsets in bytes, each 256-aligned).
 constexpr size_t kOffState = 0;                                   // RoundState + counters
-constexpr size_t kOffPairs = 1024;                                // kAlignClasses x kNaMaxPairs
-constexpr size_t kOffCut = kOffPairs + sizeof(Pair) * (size_t)kAlignClasses * kNaMaxPairs;
+constexpr size_t kOffPairs = 1024;                                // kSysClasses x kNaMaxPairs
+constexpr size_t kOffCut = kOffPairs + sizeof(Pair) * (size_t)kSysClasses * kNaMaxPairs;
 constexpr size_t kOffCluster = kOffCut + sizeof(int32_t) * (size_t)kNaMaxSeqs;
 constexpr size_t kScratchBytes = kOffCluster + sizeof(int32_t) * (size_t)kNaMaxSeqs;
 static_assert(sizeof(RoundState) + 64 * sizeof(int) <= kOffPairs, "state area too small");

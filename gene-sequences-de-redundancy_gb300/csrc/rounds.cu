@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include "gsdr_device.cuh"
+#include "lcs_band.cuh"
 #include "lcs_sys.cuh"
 
 namespace gsdr {
@@ -47,6 +48,12 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kFilterThreads = 256;
 constexpr int kAlignThreads = 256;  // 8 warps: 8/G groups of G warps
 constexpr int kAbsorbHigh = 64;     // absorbed reads per representative that shrink R
+// Largest band window (words) sent to the banded kernel: batched passes, plain
+// rounds.  A plain round waits for its slowest pair, and a lane works through
+// its pair alone, so the plain form keeps long pairs on the systolic kernels.
+constexpr int kBandMaxW = 32;
+constexpr int kPlainBandMaxW = 0;
+constexpr long long kBandMaxSerial = 16384;  // text bases x window words of one lane's pair
 
 __device__ __forceinline__ bool prefilter_pass(const int4 a, const int4 b, int cut) {
     const int s = min(a.x, b.x) + min(a.y, b.y) + min(a.z, b.z) + min(a.w, b.w);
@@ -68,9 +75,28 @@ __device__ __forceinline__ int align_class(int words) {
                                                              : words <= 512 ? 4 : 5;
 }
 
+// Queue of a pair: a band class (kSysClasses + 0..3 for windows of 4, 8, 16,
+// 32 words) when its band fits a window of at most band_max_w words, else the
+// systolic length class of its pattern.  Pairs decided without alignment
+// (trivial_decision) stay in the systolic classes, which decide them.
+// A lane works through its pair alone, so only pairs whose serial work (text
+// bases x window words) stays below kBandMaxSerial go to the banded kernel; a
+// longer one would hold up its pass.
+__device__ __forceinline__ int pair_class(int T, int q, int c, int band_max_w) {
+    if (band_max_w > 0 && T > 0 && c > 0 && q >= c && T >= c) {
+        const int bw = band_words(T, q, c);
+        if (bw <= band_max_w) {
+            const int w = bw <= 4 ? 4 : bw <= 8 ? 8 : bw <= 16 ? 16 : 32;
+            if ((long long)T * w <= kBandMaxSerial)
+                return kSysClasses + (w == 4 ? 0 : w == 8 ? 1 : w == 16 ? 2 : 3);
+        }
+    }
+    return align_class((q + 31) >> 5);
+}
+
 __device__ __forceinline__ void push_pair(RoundState* st, Pair* pairs, int seg_cap,
-                                          const DevReads& R, int rep, int q) {
-    const int cls = align_class((R.len_gf[q] + 31) >> 5);
+                                          const DevReads& R, int rep, int q, int band_max_w) {
+    const int cls = pair_class(R.len_gf[rep], R.len_gf[q], R.cut_base[q], band_max_w);
     const int slot = atomicAdd(&st->n_pairs[cls], 1);
     if (slot < seg_cap) pairs[(size_t)cls * seg_cap + slot] = Pair{rep, q};
     else st->pair_overflow = 1;
@@ -159,7 +185,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
             if (!pass) continue;
         }
         n_al++;
-        if (lane == 0) push_pair(st, pairs, seg_cap, R, rep, q);
+        if (lane == 0) push_pair(st, pairs, seg_cap, R, rep, q, kPlainBandMaxW);
     }
     if (lane == 0) {
         if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
@@ -423,6 +449,80 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, R
     if (lane == 0 && cells) atomicAdd(&st->cells, cells);
 }
 
+// Banded alignment (lcs_band.cuh) of the pairs of band class cls, whose band
+// fits a window of W words: one pair per lane.  All lanes of a warp run the
+// same blocks of 32 text bases, each on its own pair; a lane whose pair is
+// decided takes the next one from the class queue at the next block.
+template <int W, bool BATCH>
+__global__ void __launch_bounds__(kAlignThreads) k_band(DevReads R, RoundState* st, AlignArgs A,
+                                                        int cls) {
+    // text bases per unrolled group: fewer for wide windows (code size)
+    constexpr int G = W >= 16 ? 4 : 8;
+    if (st->done) return;
+    if (BATCH && (st->pair_overflow || st->n_tent == 0)) return;
+    const int np = min(st->n_pairs[cls], A.seg_cap);
+    if (np <= 0) return;
+    const int pass = BATCH ? st->pass : 0;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const Pair* list = A.pairs + (size_t)cls * A.seg_cap;
+    int* work = A.work + cls;
+    BandLane<W> L;
+    L.clear();
+    Pair p{-1, -1};
+    bool busy = false, more = true;
+    unsigned long long cells = 0;
+    unsigned acc = 0;
+    while (true) {
+        // lanes without a pair take the next ones (one atomic per warp)
+        unsigned need = __ballot_sync(kFull, !busy);
+        while (need && more) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(work, __popc(need));
+            base = __shfl_sync(kFull, base, 0);
+            if (!busy) {
+                const int i = base + __popc(need & lt_mask);
+                if (i < np) {
+                    const Pair pp = list[i];
+                    if (pp.rep >= 0) {  // not already accepted by k_greedy
+                        p = pp;
+                        L.start(R.packed + R.pack_off[pp.cand], R.len_gf[pp.cand],
+                                R.packed + R.pack_off[pp.rep], R.len_gf[pp.rep],
+                                R.cut_base[pp.cand]);
+                        busy = true;
+                    }
+                }
+            }
+            if (base + __popc(need) >= np) more = false;
+            need = __ballot_sync(kFull, !busy);
+        }
+        if (!__any_sync(kFull, busy)) break;
+        // one block of 32 text bases; an idle lane runs it with no bases
+        uint32_t tw0 = 0, tw1 = 0;
+        if (busy) {
+            if (L.x0 < L.T) tw0 = __ldg(L.pt + (L.x0 >> 4));
+            if (L.x0 + 16 < L.T) tw1 = __ldg(L.pt + (L.x0 >> 4) + 1);
+        }
+#pragma unroll 1
+        for (int j0 = 0; j0 < 32; j0 += G) L.template steps<G>(j0 < 16 ? tw0 : tw1, j0);
+        if (busy) {
+            const int d = L.finish_block();
+            if (d >= 0) {
+                cells += (unsigned long long)L.T * (unsigned long long)L.q;
+                if (d) {
+                    acc++;
+                    on_accept<BATCH>(st, A, p, pass);
+                }
+                busy = false;
+                L.T = 0;
+            }
+        }
+    }
+    acc = (unsigned)warp_sum_i((int)acc);
+    if (!BATCH && lane == 0 && acc) atomicAdd(&st->cnt_accepted, (unsigned long long)acc);
+    if (cells) atomicAdd(&st->cells, cells);
+}
+
 __global__ void k_compact(RoundState* st, const int32_t* __restrict__ remain_in,
                           int32_t* __restrict__ remain_out, const int32_t* __restrict__ cluster) {
     if (st->done) return;
@@ -457,7 +557,7 @@ __device__ void reset_align_counters(RoundState* st, int* align_work) {
         st->n_pairs[c] = 0;
         align_work[c] = 0;
     }
-    align_work[6] = 0;  // k_align_single's shared queue
+    align_work[kSingleWorkSlot] = 0;  // k_align_single's shared queue
 }
 
 __global__ void k_advance(RoundState* st, int32_t* cluster, int* align_work) {
@@ -640,7 +740,8 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundSta
                 }
                 mask = pass_mask;
             }
-            if (lane < ng && (mask & (1u << lane))) push_pair(st, pairs, seg_cap, R, ttent[lane], q);
+            if (lane < ng && (mask & (1u << lane)))
+                push_pair(st, pairs, seg_cap, R, ttent[lane], q, kBandMaxW);
             n_al += __popc(mask);
         }
     }
@@ -928,7 +1029,7 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
                     n_wf++;
                     const int rep = s_tent[t];
                     if (prefilter_pass(R.comp[rep], R.comp[q], R.cut_base[q])) {
-                        push_pair(st, pairs, seg_cap, R, rep, q);
+                        push_pair(st, pairs, seg_cap, R, rep, q, kBandMaxW);
                         n_al++;
                     }
                 }
@@ -1080,7 +1181,7 @@ __global__ void k_init(RoundState* st, int32_t* cluster, int32_t* remain, uint32
         s.R = 1;
         s.R_max = r_max;
         *st = s;
-        for (int c = 0; c < kAlignClasses + 1; c++) align_work[c] = 0;
+        for (int c = 0; c <= kSingleWorkSlot; c++) align_work[c] = 0;
     }
 }
 
@@ -1212,9 +1313,28 @@ void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s)
     k_align<G, W, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
 }
 
+template <int W, bool BATCH>
+void launch_band_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
+    static int grid = 0;
+    if (!grid) grid = grid_for(k_band<W, BATCH>, kAlignThreads, 0, 8);
+    k_band<W, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
+}
+
+// Kernels launch_align_classes launches (after the greedy bound).
+template <bool BATCH>
+constexpr int align_launches() {
+    return kSysClasses - (BATCH ? 3 : 0) + (BATCH || kPlainBandMaxW > 0 ? kBandClasses : 0);
+}
+
 template <bool BATCH>
 void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bool greedy = true) {
     if (greedy) k_greedy<BATCH><<<num_sms() * 8, 256, 0, s>>>(R, B.st, align_args(B));
+    if (BATCH || kPlainBandMaxW > 0) {
+        launch_band_t<4, BATCH>(R, B, kSysClasses + 0, s);
+        launch_band_t<8, BATCH>(R, B, kSysClasses + 1, s);
+        launch_band_t<16, BATCH>(R, B, kSysClasses + 2, s);
+        launch_band_t<32, BATCH>(R, B, kSysClasses + 3, s);
+    }
     if constexpr (!BATCH) {
         launch_align_t<1, 1, BATCH>(R, B, 0, s);
         launch_align_t<1, 2, BATCH>(R, B, 1, s);
@@ -1222,9 +1342,9 @@ void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bo
     if constexpr (BATCH) {
         static int grid = 0;
         if (!grid) grid = grid_for(k_align_single, kAlignThreads, 0, 8);
-        // the single-warp classes share work counter slot 6
-        k_align_single<<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B),
-                                                      reinterpret_cast<int*>(B.st + 1) + 6);
+        // the single-warp classes share one work counter
+        k_align_single<<<grid, kAlignThreads, 0, s>>>(
+            R, B.st, align_args(B), reinterpret_cast<int*>(B.st + 1) + kSingleWorkSlot);
         launch_align_t<2, 8, BATCH>(R, B, 4, s);
         launch_align_t<4, 8, BATCH>(R, B, 5, s);
     } else {
@@ -1261,7 +1381,7 @@ void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 4 + kAlignClasses;
+    if (count) *count += 4 + align_launches<false>();
 }
 
 void launch_align_stage(const DevReads& R, RoundBuffers& B, bool batched_mapping, bool greedy,
@@ -1293,7 +1413,7 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 8 + kAlignClasses - 3 + (!drop && B.idx_off ? 1 : 0);
+    if (count) *count += 8 + align_launches<true>() + (!drop && B.idx_off ? 1 : 0);
 }
 
 // Whether a job's per-pass k-mer index (at most `cap` postings) is kept in

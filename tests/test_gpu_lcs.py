@@ -1,7 +1,8 @@
 """Alignment kernels alone against the oracle's LCS: the decision
 LCS(pattern, text) >= ceil(len(pattern) * t) (kernel_align,
 cuda-version/func.cu:828-999) for random, mutated and repetitive pairs in
-every length class, with both warp groupings and with the greedy bound."""
+every length class, with both warp groupings, with the banded one-pair-per-lane
+kernel (mapping 2) and with the greedy bound."""
 import numpy as np
 import pytest
 
@@ -80,7 +81,7 @@ def build_case(rng, n_pairs, qlen, tlen, kind):
     return seqs, pairs
 
 
-@pytest.mark.parametrize("mapping", [0, 1])
+@pytest.mark.parametrize("mapping", [0, 1, 2])
 @pytest.mark.parametrize("greedy", [0, 1])
 @pytest.mark.parametrize("qlen,tlen,kind", [
     ((20, 1000), (20, 1200), "mutated"),        # classes 0-1
@@ -117,7 +118,29 @@ def test_lcs_edge_lengths():
     seqs.append(b)
     seqs.append(b[:200] + b"NNNNNNNNNN" + b[200:400])
     pairs.append((len(seqs) - 1, len(seqs) - 2))
-    for mapping in (0, 1):
+    for mapping in (0, 1, 2):
         for t in (0.8, 0.9, 0.95):
             got, _ = gsdr.lcs_decide(seqs, pairs, t, mapping=mapping, greedy=1)
             np.testing.assert_array_equal(got, expected(seqs, pairs, t))
+
+
+@pytest.mark.parametrize("t", [0.80, 0.90, 0.95, 0.99])
+@pytest.mark.parametrize("qlen", [(30, 400), (400, 3000), (3000, 12000)])
+def test_band_near_threshold(t, qlen):
+    """Pairs of similar length whose identity straddles t: every window class
+    of the banded kernel (4 to 32 words) decides them as the full DP does."""
+    rng = np.random.default_rng(int(t * 100) * 7 + qlen[0])
+    seqs, pairs = [], []
+    n = 40 if qlen[0] >= 3000 else 150
+    for _ in range(n):
+        T = int(rng.integers(*qlen))
+        b = rand_seq(rng, T)
+        a = mutate(rng, b, rng.uniform(0.0, 2.2 * (1 - t) + 0.005), indel=0.4)
+        seqs.append(b)
+        seqs.append(a)
+        pairs.append((len(seqs) - 1, len(seqs) - 2))
+    want = expected(seqs, pairs, t)
+    assert 0 < want.sum() < len(pairs)
+    got, _ = gsdr.lcs_decide(seqs, pairs, t, mapping=2, greedy=0)
+    bad = np.nonzero(got != want)[0]
+    assert len(bad) == 0, f"{len(bad)} of {len(pairs)} differ, first {bad[:5]}"
