@@ -69,6 +69,7 @@ struct Plan {
     int r_max = 1;          // largest R (tentatives per pass)
     int64_t idx_cap = 0;    // > 0: batched word filter by inverted index, postings capacity
     bool idx_smem = false;  // that index fits the filter's shared memory (16-bit copy)
+    bool bits = false;      // batched word filter by k-mer presence bitmaps
 };
 
 constexpr int kSmemOptin = 227 * 1024;  // per-block shared memory limit of sm_100 / sm_103
@@ -115,9 +116,15 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
     }
     if (o.batch != 1 && !drop && n > 0) {
         bool index = ents_sum * kIndexDensity <= kcap * (int64_t)n;
+        // the bitmap bound decides almost every pair of short reads but
+        // almost none once reads hold most of the 4^k k-mers (long reads at
+        // k = 6): automatic only below a quarter of the k-mer space
+        bool bits = !index && k <= kMaxBitsK && ents_sum * 4 <= kcap * (int64_t)n;
         const char* f = std::getenv("GSDR_BFILTER");
-        if (f && std::strcmp(f, "index") == 0) index = true;
-        if (f && std::strcmp(f, "table") == 0) index = false;
+        if (f && std::strcmp(f, "index") == 0) index = true, bits = false;
+        if (f && std::strcmp(f, "table") == 0) index = false, bits = false;
+        if (f && std::strcmp(f, "bits") == 0) index = false, bits = k <= kMaxBitsK;
+        P.bits = bits;
         if (index) {
             // a pass indexes at most R_max tentatives: for length-sorted reads
             // those hold at most the first R_max reads' entries
@@ -185,6 +192,7 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     // 16-byte copies read whole: both rounded up to 8 entries
     B.idx_off16 = P.idx_smem ? c.take<uint16_t>(((size_t)1 << (2 * k)) + 8) : nullptr;
     B.idx_post16 = P.idx_smem ? c.take<uint16_t>((size_t)P.idx_cap + 8) : nullptr;
+    B.amb = P.bits ? c.take<Pair>((size_t)B.seg_cap) : nullptr;
     return c.used + 256;
 }
 
@@ -268,7 +276,7 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     JCUDA(cudaMalloc(&dmem_, dbytes_));
     carve_all(reinterpret_cast<char*>(dmem_), n, n_bytes_, P, opts.drop == 1, opts.word_length,
               R_, B_);
-    stats.word_index = P.idx_cap > 0 ? 1 : 0;
+    stats.word_index = P.idx_cap > 0 ? 1 : (P.bits ? 2 : 0);
     pack_off_.swap(P.pack_off);
     kmer_off_.swap(P.kmer_off);
     return GSDR_OK;

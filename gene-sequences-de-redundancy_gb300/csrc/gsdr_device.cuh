@@ -76,6 +76,7 @@ struct RoundState {
     int32_t acc_overflow;
     int32_t survivors;  // representatives confirmed this pass
     int32_t absorbed;   // reads absorbed this pass
+    int32_t n_amb;      // pairs the bitmap bound left to the exact word filter
     long long rounds;   // representatives taken so far
     long long passes;
     unsigned long long cnt_prefilter, cnt_word, cnt_aligned, cnt_accepted;
@@ -123,6 +124,9 @@ struct RoundBuffers {
     uint16_t* idx_post16;
     int64_t idx_cap;
     int32_t r_max;       // largest R of the job (sizes the index filter's shared memory)
+    // batched word filter by k-mer presence bitmaps (k <= kMaxBitsK; null =
+    // another form): pairs the bound D <= S <= D + min(excess) cannot decide
+    Pair* amb;           // seg_cap pairs
 };
 void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s);
 // One plain round (filter, align, compact, advance); `parity` picks which

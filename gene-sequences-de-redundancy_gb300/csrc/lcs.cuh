@@ -115,6 +115,55 @@ __device__ __forceinline__ void hyyro_step(uint32_t (&V)[W], const uint32_t (&H)
     }
 }
 
+// The same step with the match masks read from a table in shared memory
+// instead of formed from the bit planes (that moves two logic operations per
+// word off the integer pipe, which bounds these kernels): pm[32 * i] is the
+// match mask of word i for this step's base (one lane's row of the table);
+// inv is all ones for "no base" (U = 0).
+template <int W>
+__device__ __forceinline__ void peq_step(uint32_t (&V)[W], const uint32_t* __restrict__ pm,
+                                         uint32_t inv, uint32_t& cy) {
+    constexpr int C = W >= 4 ? 4 : W;
+#pragma unroll
+    for (int i = 0; i < W; i += C) {
+        uint32_t m[C], u[C], s[C];
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            m[j] = pm[32 * (i + j)];
+            u[j] = V[i + j] & m[j] & ~inv;
+        }
+        if constexpr (C == 4)
+            add4_carry(s[0], s[1], s[2], s[3], V[i], V[i + 1], V[i + 2], V[i + 3], u[0], u[1],
+                       u[2], u[3], cy);
+        else if constexpr (C == 2)
+            add2_carry(s[0], s[1], V[i], V[i + 1], u[0], u[1], cy);
+        else
+            add1_carry(s[0], V[i], u[0], cy);
+#pragma unroll
+        for (int j = 0; j < C; j++) V[i + j] = s[j] | (V[i + j] & ~m[j]);
+    }
+}
+
+// Match-mask table of one lane's W pattern words: peq[(b * W + i) * 32] =
+// positions of word i holding base b (b = 0..3; lane-interleaved, so a warp's
+// lanes read consecutive words).  Positions past the pattern match base 0,
+// as the zero bit planes do in hyyro_step; their carries only move upward
+// and their bits are never counted.
+template <int W>
+__device__ __forceinline__ void peq_fill(uint32_t* peq, const uint32_t* __restrict__ pq, int q,
+                                         int w0) {
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        const int w = w0 + i;
+        uint32_t h = 0, l = 0;
+        if (w * 32 < q) planes32(__ldg(pq + 2 * w), __ldg(pq + 2 * w + 1), h, l);
+        peq[(0 * W + i) * 32] = ~h & ~l;
+        peq[(1 * W + i) * 32] = ~h & l;
+        peq[(2 * W + i) * 32] = h & ~l;
+        peq[(3 * W + i) * 32] = h & l;
+    }
+}
+
 __device__ __forceinline__ int warp_sum_i(int v) {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);

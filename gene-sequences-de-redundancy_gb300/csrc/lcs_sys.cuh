@@ -12,9 +12,10 @@
 // top lane's carry-out sequence (one bit per text base) is the next warp's
 // lane-0 carry-in sequence, handed over in 32-bit words through a ring in
 // shared memory.  Text bases come from a per-warp 64-entry ring (written twice
-// so that a lane-skewed window is contiguous), one 32-bit word per base whose
-// bytes hold the sign-coded high bit, low bit and "no base" flag; prmt turns
-// each byte into a full mask.
+// so that a lane-skewed window is contiguous), one 32-bit word per base: its
+// 2-bit code and a "no base" flag in bit 31.  A step reads its match masks
+// from the lane's row of a per-warp table in shared memory indexed by the code
+// (peq_step), which keeps the integer pipe for the recurrence itself.
 //
 // Bases outside the text ("no base": pipeline fill before base 0, drain after
 // base T-1) must leave V unchanged.  The flag only clears U: with U = 0 and a
@@ -84,18 +85,9 @@ __device__ __forceinline__ int zeros_below(const uint32_t (&V)[W], int w0, int l
     return z;
 }
 
-// Replicates the sign bit of byte `SEL` of x into all 32 bits.
-template <int SEL>
-__device__ __forceinline__ uint32_t sign_mask(uint32_t x) {
-    uint32_t r;
-    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "n"(0x8888 | (SEL * 0x1111)));
-    return r;
-}
-
-// Sign-coded text base: byte 0 = high bit, byte 1 = low bit, byte 2 = no base.
+// Ring entry of a text base: the 2-bit code, bit 31 set for "no base".
 __device__ __forceinline__ uint32_t base_word(uint32_t code, bool valid) {
-    if (!valid) return 0x00800000u;
-    return ((code & 2u) ? 0x80u : 0u) | ((code & 1u) ? 0x8000u : 0u);
+    return valid ? (code & 3u) : 0x80000000u;
 }
 
 __device__ __forceinline__ void sys_fail(SysGroup& S, int* err_flag, int lane) {
@@ -113,17 +105,17 @@ __device__ __forceinline__ void sys_fail(SysGroup& S, int* err_flag, int lane) {
 //   SNAP:  lane l copies V into snapV after the step j == tj (per lane).
 template <int W, bool MULTI, bool SNAP>
 __device__ __forceinline__ void sys_steps8(const uint32_t* __restrict__ rb,
-                                           const uint32_t (&H)[W], const uint32_t (&Lo)[W],
-                                           uint32_t (&V)[W], uint32_t (&snapV)[W],
-                                           uint32_t& from, uint32_t cin8, uint32_t& out8,
-                                           uint32_t not_lane0, int tj, int jbase, int lane) {
+                                           const uint32_t* __restrict__ peq, uint32_t (&V)[W],
+                                           uint32_t (&snapV)[W], uint32_t& from, uint32_t cin8,
+                                           uint32_t& out8, uint32_t not_lane0, int tj, int jbase,
+                                           int lane) {
 #pragma unroll
     for (int j = 0; j < 8; j++) {
         uint32_t cin = from;
         if (MULTI) cin = not_lane0 ? from : ((cin8 >> j) & 1u);
         const uint32_t b = rb[j];
-        const uint32_t ch = sign_mask<0>(b), cl = sign_mask<1>(b), inv = sign_mask<2>(b);
-        hyyro_step<W>(V, H, Lo, ch, cl, ~inv, cin);
+        const uint32_t inv = (uint32_t)((int32_t)b >> 31);
+        peq_step<W>(V, peq + (b & 3u) * (32u * W), inv, cin);
         if (MULTI) out8 |= cin << j;
         // lane 0 receives its own carry-out from the shuffle: a single warp
         // clears it (its lane-0 carry-in is zero); a group member ignores it
@@ -138,8 +130,8 @@ __device__ __forceinline__ void sys_steps8(const uint32_t* __restrict__ rb,
 
 // One block of 32 steps (four unrolled groups of eight).
 template <int W, bool MULTI, bool SNAP>
-__device__ __forceinline__ void sys_block(const uint32_t* __restrict__ rb, const uint32_t (&H)[W],
-                                          const uint32_t (&Lo)[W], uint32_t (&V)[W],
+__device__ __forceinline__ void sys_block(const uint32_t* __restrict__ rb,
+                                          const uint32_t* __restrict__ peq, uint32_t (&V)[W],
                                           uint32_t (&snapV)[W], uint32_t& from, uint32_t cin_word,
                                           uint32_t& cout_word, uint32_t not_lane0, int tj,
                                           int lane) {
@@ -147,28 +139,29 @@ __device__ __forceinline__ void sys_block(const uint32_t* __restrict__ rb, const
 #pragma unroll 1
     for (int g = 0; g < 4; g++) {
         uint32_t out8 = 0;
-        sys_steps8<W, MULTI, SNAP>(rb + 8 * g, H, Lo, V, snapV, from, cin_word >> (8 * g), out8,
+        sys_steps8<W, MULTI, SNAP>(rb + 8 * g, peq, V, snapV, from, cin_word >> (8 * g), out8,
                                    not_lane0, tj, 8 * g, lane);
         if (MULTI) cout_word |= out8 << (8 * g);
     }
 }
 
+// Shared memory of one warp's match-mask table (sys_peq_words(W) words).
+__host__ __device__ constexpr int sys_peq_words(int W) { return 4 * W * 32; }
+
 // The decision of one pair on B warps of a group (gw = this warp's index).
 // The result lands in S.result (1 accept, 0 reject) once the group meets at
-// its barrier; S.error is set if a wait gave up.
+// its barrier; S.error is set if a wait gave up.  peq: this warp's
+// sys_peq_words(W) words of shared memory for the pattern's match masks.
 template <int W>
-__device__ void lcs_sys_pair(SysGroup& S, const uint32_t* __restrict__ pq, int q,
+__device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restrict__ pq, int q,
                              const uint32_t* __restrict__ pt, int T, int c, int B, int gw,
                              int lane, int* err_flag) {
     const int w0 = (gw * 32 + lane) * W;
-    uint32_t H[W], Lo[W], V[W], snapV[W];
+    uint32_t V[W], snapV[W];
+    peq += lane;
+    peq_fill<W>(peq, pq, q, w0);
 #pragma unroll
     for (int i = 0; i < W; i++) {
-        const int w = w0 + i;
-        uint32_t hi = 0, lo = 0;
-        if (w * 32 < q) planes32(__ldg(pq + 2 * w), __ldg(pq + 2 * w + 1), hi, lo);
-        H[i] = hi;
-        Lo[i] = lo;
         V[i] = 0xffffffffu;
         snapV[i] = 0xffffffffu;
     }
@@ -216,17 +209,17 @@ __device__ void lcs_sys_pair(SysGroup& S, const uint32_t* __restrict__ pq, int q
         if (phase == kSysCk - 1 || (phase == 0 && m > 0)) {
             const int tj = phase == 0 ? (lane == 0 ? -1 : lane - 1) : (lane == 0 ? 31 : -1);
             if (multi)
-                sys_block<W, true, true>(rb, H, Lo, V, snapV, from, cin_word, cout_word, not_lane0,
+                sys_block<W, true, true>(rb, peq, V, snapV, from, cin_word, cout_word, not_lane0,
                                          tj, lane);
             else
-                sys_block<W, false, true>(rb, H, Lo, V, snapV, from, cin_word, cout_word,
+                sys_block<W, false, true>(rb, peq, V, snapV, from, cin_word, cout_word,
                                           not_lane0, tj, lane);
         } else {
             if (multi)
-                sys_block<W, true, false>(rb, H, Lo, V, snapV, from, cin_word, cout_word,
+                sys_block<W, true, false>(rb, peq, V, snapV, from, cin_word, cout_word,
                                           not_lane0, -1, lane);
             else
-                sys_block<W, false, false>(rb, H, Lo, V, snapV, from, cin_word, cout_word,
+                sys_block<W, false, false>(rb, peq, V, snapV, from, cin_word, cout_word,
                                            not_lane0, -1, lane);
         }
         __syncwarp();

@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
                                                          int cls) {
     constexpr int NG = (kAlignThreads / 32) / G;
     __shared__ SysGroup groups[NG];
+    extern __shared__ __align__(16) uint32_t peq_all[];  // sys_peq_words(W) per warp
     if (st->done) return;
     if (BATCH && (st->pair_overflow || st->n_tent == 0)) return;
     const int np = min(st->n_pairs[cls], A.seg_cap);
@@ -362,8 +363,9 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
             const int words = (q + 31) >> 5;
             const int B = (words + 32 * W - 1) / (32 * W);
             if (gw < B)
-                lcs_sys_pair<W>(S, R.packed + R.pack_off[p.cand], q, R.packed + R.pack_off[p.rep],
-                                 T, c, B, gw, lane, &st->error);
+                lcs_sys_pair<W>(S, peq_all + warp * sys_peq_words(W),
+                                R.packed + R.pack_off[p.cand], q, R.packed + R.pack_off[p.rep], T,
+                                c, B, gw, lane, &st->error);
         }
         group_bar(bar_id, bar_n);
         if (gw == 0 && lane == 0) {
@@ -396,6 +398,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
 __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, RoundState* st,
                                                                    AlignArgs A, int* work) {
     __shared__ SysGroup groups[kAlignThreads / 32];
+    extern __shared__ __align__(16) uint32_t peq_all[];  // sys_peq_words(8) per warp
     if (st->done) return;
     if (st->pair_overflow || st->n_tent == 0) return;
     int cnt[4], total = 0;
@@ -432,11 +435,12 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, R
             __syncwarp();
             const uint32_t* pq = R.packed + R.pack_off[p.cand];
             const uint32_t* pt = R.packed + R.pack_off[p.rep];
+            uint32_t* peq = peq_all + warp * sys_peq_words(8);
             switch (cls) {
-                case 0: lcs_sys_pair<1>(S, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 1: lcs_sys_pair<2>(S, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 2: lcs_sys_pair<4>(S, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                default: lcs_sys_pair<8>(S, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 0: lcs_sys_pair<1>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 1: lcs_sys_pair<2>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 2: lcs_sys_pair<4>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                default: lcs_sys_pair<8>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
             }
             __syncwarp();
             ok = *(volatile int*)&S.error ? 0 : *(volatile int*)&S.result;
@@ -631,6 +635,7 @@ __global__ void __launch_bounds__(1024) k_bselect(RoundState* st, const int32_t*
     if (threadIdx.x == 0) {
         st->n_tent = nt;
         st->n_acc = 0;
+        st->n_amb = 0;
         st->acc_overflow = 0;
         st->pair_overflow = 0;
         st->survivors = 0;
@@ -749,6 +754,175 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundSta
     if (lane == 0) {
         if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
         if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
+        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
+        if (bytes) atomicAdd(&st->filter_bytes, bytes);
+    }
+}
+
+// ---- word filter by k-mer presence bitmaps (k <= kMaxBitsK) ----------------
+//
+// With D = the number of k-mers both reads hold (non-zero stored counts) and
+// E = a read's count excess (sum of counts minus distinct k-mers), the word
+// sum S of kernel_filter (func.cu:803-826) satisfies D <= S <= D + min(E_t,
+// E_q): every shared k-mer adds at least one and at most one plus its excess.
+// D is a popcount over the two 4^k-bit bitmaps, so k_bfilter_bits decides
+// almost every pair with 4^k / 32 AND + POPC per lane instead of one table
+// lookup per k-mer; the few pairs the bound leaves open go to k_bexact, which
+// forms S itself.
+
+constexpr int kBitsGroup = 64;  // tentatives staged per CTA
+
+template <int K>
+__global__ void __launch_bounds__(kFilterThreads) k_bfilter_bits(DevReads R, RoundState* st,
+                                                                 const int32_t* __restrict__ remain,
+                                                                 const int32_t* __restrict__ tent,
+                                                                 Pair* pairs, int seg_cap, Pair* amb) {
+    constexpr int NQ = (1 << (2 * K)) / 128;  // 16-byte words of a bitmap
+    constexpr int RG = kBitsGroup;
+    constexpr int WARPS = kFilterThreads / 32;
+    // tentative bitmaps as [quad][tentative]: lane t reads consecutive 16 bytes
+    __shared__ __align__(16) uint4 tb[NQ][RG];
+    __shared__ __align__(16) uint4 cb[WARPS][NQ];
+    __shared__ int4 tcomp[RG];
+    __shared__ int ttent[RG], textra[RG];
+    if (st->done || st->n_tent == 0) return;
+    const int nt = st->n_tent;
+    const int n = st->n_remain;
+    const int ngroups = (nt + RG - 1) / RG;
+    const int parts = max(1, (int)gridDim.x / ngroups);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint4* kb4 = reinterpret_cast<const uint4*>(R.kbits);
+    unsigned n_pf = 0, n_wf = 0, n_al = 0;
+    unsigned long long bytes = 0;
+    int cur_group = -1;
+    for (int item = blockIdx.x; item < ngroups * parts; item += gridDim.x) {
+        const int g = item % ngroups, part = item / ngroups;
+        const int t0 = g * RG;
+        const int ng = min(RG, nt - t0);
+        if (g != cur_group) {
+            __syncthreads();
+            if (threadIdx.x < RG) {
+                const int i = t0 + threadIdx.x;
+                const bool in = threadIdx.x < ng;
+                const int rep = in ? tent[i] : 0;
+                ttent[threadIdx.x] = in ? rep : 0x7fffffff;
+                tcomp[threadIdx.x] = in ? R.comp[rep] : make_int4(0, 0, 0, 0);
+                textra[threadIdx.x] = in ? R.kextra[rep] : 0;
+            }
+            for (int i = threadIdx.x; i < ng * NQ; i += kFilterThreads) {
+                const int t = i / NQ, w = i % NQ;
+                tb[w][t] = __ldg(kb4 + (size_t)tent[t0 + t] * NQ + w);
+            }
+            __syncthreads();
+            cur_group = g;
+        }
+        const int per = (n + parts - 1) / parts;
+        const int lo = part * per, hi = min(n, lo + per);
+        for (int idx = lo + warp; idx < hi; idx += WARPS) {
+            const int q = remain[idx];
+            const int4 cq = R.comp[q];
+            const int cbq = R.cut_base[q];
+            unsigned ok_bits[RG / 32];
+            bool any = false;
+#pragma unroll
+            for (int h = 0; h < RG / 32; h++) {
+                const int t = 32 * h + lane;
+                const bool before = t < ng && ttent[t] < q;
+                n_pf += before;
+                const bool ok = before && prefilter_pass(tcomp[t], cq, cbq);
+                ok_bits[h] = __ballot_sync(kFull, ok);
+                any |= ok_bits[h] != 0;
+            }
+            if (!any) continue;
+            for (int i = lane; i < NQ; i += 32) cb[warp][i] = __ldcs(kb4 + (size_t)q * NQ + i);
+            bytes += 16ull * NQ;
+            __syncwarp();
+            const int cw = R.cut_word[q];
+            const int exq = R.kextra[q];
+#pragma unroll
+            for (int h = 0; h < RG / 32; h++) {
+                if (!ok_bits[h]) continue;
+                const int t = 32 * h + lane;
+                int d = 0;
+#pragma unroll 8
+                for (int w = 0; w < NQ; w++) {
+                    const uint4 a = cb[warp][w];
+                    const uint4 b = tb[w][t];
+                    d += __popc(a.x & b.x) + __popc(a.y & b.y) + __popc(a.z & b.z) +
+                         __popc(a.w & b.w);
+                }
+                if ((ok_bits[h] >> lane) & 1u) {
+                    n_wf++;
+                    if (d >= cw) {
+                        push_pair(st, pairs, seg_cap, R, ttent[t], q, kBandMaxW);
+                        n_al++;
+                    } else if (d + min(textra[t], exq) >= cw) {
+                        const int slot = atomicAdd(&st->n_amb, 1);
+                        if (slot < seg_cap) amb[slot] = Pair{ttent[t], q};
+                        else st->pair_overflow = 1;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    n_pf = (unsigned)warp_sum_i((int)n_pf);
+    n_wf = (unsigned)warp_sum_i((int)n_wf);
+    n_al = (unsigned)warp_sum_i((int)n_al);
+    if (lane == 0) {
+        if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
+        if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
+        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
+        if (bytes) atomicAdd(&st->filter_bytes, bytes);
+    }
+}
+
+// The word sum S itself for the pairs k_bfilter_bits left open: one warp per
+// pair scatters the tentative's counts into a table in shared memory and
+// streams the candidate's (k-mer, count) entries against it.
+template <int K>
+__global__ void __launch_bounds__(kFilterThreads) k_bexact(DevReads R, RoundState* st,
+                                                           const Pair* __restrict__ amb,
+                                                           Pair* pairs, int seg_cap) {
+    constexpr int NB = 1 << (2 * K);
+    constexpr int WARPS = kFilterThreads / 32;
+    extern __shared__ __align__(16) uint16_t xtab[];  // [WARPS][NB]
+    if (st->done || st->n_tent == 0) return;
+    const int na = min(st->n_amb, seg_cap);
+    if (na <= 0) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint16_t* tab = xtab + warp * NB;
+    unsigned n_al = 0;
+    unsigned long long bytes = 0;
+    for (int k = blockIdx.x * WARPS + warp; k < na; k += gridDim.x * WARPS) {
+        const Pair p = amb[k];
+        uint4* t4 = reinterpret_cast<uint4*>(tab);
+        for (int i = lane; i < NB / 8; i += 32) t4[i] = make_uint4(0u, 0u, 0u, 0u);
+        __syncwarp();
+        const uint32_t* et = R.kmer + R.kmer_off[p.rep];
+        const int nt_ = R.n_kmer[p.rep];
+        for (int i = lane; i < nt_; i += 32) {
+            const uint32_t v = __ldg(et + i);
+            const uint32_t c = v & 0xffffu;
+            if (c) tab[v >> 16] = (uint16_t)c;  // kernel_makeTable: only order > 0
+        }
+        __syncwarp();
+        const uint32_t* eq = R.kmer + R.kmer_off[p.cand];
+        const int nq = R.n_kmer[p.cand];
+        int sum = 0;
+        for (int i = lane; i < nq; i += 32) {
+            const uint32_t v = __ldg(eq + i);
+            sum += min((uint32_t)tab[v >> 16], v & 0xffffu);
+        }
+        bytes += 4ull * (unsigned)(nt_ + nq);
+        sum = warp_sum_i(sum);
+        if (!(sum < R.cut_word[p.cand])) {
+            if (lane == 0) push_pair(st, pairs, seg_cap, R, p.rep, p.cand, kBandMaxW);
+            n_al++;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
         if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
         if (bytes) atomicAdd(&st->filter_bytes, bytes);
     }
@@ -1259,9 +1433,32 @@ void launch_bfilter_idx_t(const DevReads& R, RoundBuffers& B, const int32_t* rem
     }
 }
 
+template <int K>
+void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
+                           cudaStream_t s) {
+    const int xsmem = (kFilterThreads / 32) * (1 << (2 * K)) * 2;
+    static int grid = 0, xgrid = 0;
+    if (!grid) {
+        cudaFuncSetAttribute(k_bexact<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, xsmem);
+        grid = grid_for(k_bfilter_bits<K>, kFilterThreads, 0, 8);
+        xgrid = grid_for(k_bexact<K>, kFilterThreads, xsmem, 8);
+    }
+    k_bfilter_bits<K><<<grid, kFilterThreads, 0, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap,
+                                                      B.amb);
+    k_bexact<K><<<xgrid, kFilterThreads, xsmem, s>>>(R, B.st, B.amb, B.pairs, B.seg_cap);
+}
+
 template <bool BATCH>
 void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain, int drop,
                        cudaStream_t s) {
+    if (BATCH && !drop && B.amb) {
+        switch (R.k) {
+            case 4: launch_bfilter_bits_t<4>(R, B, remain, s); break;
+            case 5: launch_bfilter_bits_t<5>(R, B, remain, s); break;
+            default: launch_bfilter_bits_t<6>(R, B, remain, s); break;
+        }
+        return;
+    }
     if (BATCH && !drop && B.idx_off) {
         switch (R.k) {
             case 4: launch_bfilter_idx_t<4>(R, B, remain, s); break;
@@ -1308,9 +1505,14 @@ AlignArgs align_args(RoundBuffers& B) {
 
 template <int G, int W, bool BATCH>
 void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
+    constexpr int smem = (kAlignThreads / 32) * sys_peq_words(W) * 4;
     static int grid = 0;
-    if (!grid) grid = grid_for(k_align<G, W, BATCH>, kAlignThreads, 0, 8);
-    k_align<G, W, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
+    if (!grid) {
+        cudaFuncSetAttribute(k_align<G, W, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+        grid = grid_for(k_align<G, W, BATCH>, kAlignThreads, smem, 8);
+    }
+    k_align<G, W, BATCH><<<grid, kAlignThreads, smem, s>>>(R, B.st, align_args(B), cls);
 }
 
 template <int W, bool BATCH>
@@ -1340,10 +1542,15 @@ void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bo
         launch_align_t<1, 2, BATCH>(R, B, 1, s);
     }
     if constexpr (BATCH) {
+        constexpr int smem = (kAlignThreads / 32) * sys_peq_words(8) * 4;
         static int grid = 0;
-        if (!grid) grid = grid_for(k_align_single, kAlignThreads, 0, 8);
+        if (!grid) {
+            cudaFuncSetAttribute(k_align_single, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+            grid = grid_for(k_align_single, kAlignThreads, smem, 8);
+        }
         // the single-warp classes share one work counter
-        k_align_single<<<grid, kAlignThreads, 0, s>>>(
+        k_align_single<<<grid, kAlignThreads, smem, s>>>(
             R, B.st, align_args(B), reinterpret_cast<int*>(B.st + 1) + kSingleWorkSlot);
         launch_align_t<2, 8, BATCH>(R, B, 4, s);
         launch_align_t<4, 8, BATCH>(R, B, 5, s);
@@ -1413,7 +1620,7 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 8 + align_launches<true>() + (!drop && B.idx_off ? 1 : 0);
+    if (count) *count += 8 + align_launches<true>() + (!drop && (B.idx_off || B.amb) ? 1 : 0);
 }
 
 // Whether a job's per-pass k-mer index (at most `cap` postings) is kept in

@@ -76,8 +76,10 @@ typedef struct {
     double ms_filter, ms_align; /* with stage_timing only */
     int32_t k, drop, pigeon, batch;
     int64_t kernel_launches;  /* kernels launched by the library during the call */
-    int32_t word_index;       /* 1: the batched word filter used the per-pass inverted
-                                 k-mer index (reads holding few of the 4^k k-mers) */
+    int32_t word_index;       /* form of the batched word filter: 0 per-tentative k-mer
+                                 tables, 1 per-pass inverted k-mer index (reads holding
+                                 few of the 4^k k-mers), 2 k-mer presence bitmaps with
+                                 an exact sum for the pairs their bound leaves open */
 } gsdr_stats;
 
 /* Fill `o` with the reference defaults (t 0.95, derived k/drop, pigeon 0). */

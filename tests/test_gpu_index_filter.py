@@ -1,8 +1,9 @@
-"""Batched word filter by per-pass inverted k-mer index (chosen automatically
-for reads holding few of the 4^k k-mers, e.g. 150 bp reads at k = 7) against
-the oracle: identical cluster arrays and FASTA bytes, in both filter forms, at
-every R, every word length, and for reads too short to hold a k-mer (the
-reference's kernel_filter, cuda-version/func.cu:803-826)."""
+"""Batched word filter forms against the oracle: the per-pass inverted k-mer
+index (chosen for reads holding few of the 4^k k-mers, e.g. 150 bp reads at
+k = 7), the k-mer presence bitmaps (k <= 6 otherwise) and the per-tentative
+tables.  Identical cluster arrays and FASTA bytes in every form, at every R,
+every word length, and for reads too short to hold a k-mer (the reference's
+kernel_filter, cuda-version/func.cu:803-826)."""
 import numpy as np
 import pytest
 
@@ -97,3 +98,55 @@ def test_index_form_is_repeatable(monkeypatch):
         job.close()
         f.close()
     assert np.array_equal(a, b)
+
+
+# ---- k-mer presence bitmaps (k <= 6): bound D <= S <= D + min(excess), exact
+# sum for the pairs it leaves open
+
+@pytest.mark.parametrize("batch", [2, 64, 256, 0])
+def test_c0_recipe_bits_auto(tmp_path, monkeypatch, batch):
+    # 200-1000 bp reads hold a small part of the 4^6 k-mers: bitmaps chosen
+    data = gsdr.synth_fasta(0, n_reads=4000, seed=40)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, batch, None)
+    assert st.k == 6 and st.word_index == 2
+
+
+@pytest.mark.parametrize("batch", [2, 256])
+def test_c1_recipe_bits_forced(tmp_path, monkeypatch, batch):
+    # long reads: the bound leaves most pairs open (exact sums, queue refills)
+    data = gsdr.synth_fasta(1, n_reads=8000, seed=41)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, batch, "bits")
+    assert st.k == 6 and st.word_index == 2
+
+
+def test_c1_recipe_tables_auto(tmp_path, monkeypatch):
+    data = gsdr.synth_fasta(1, n_reads=8000, seed=41)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 0, None)
+    assert st.k == 6 and st.word_index == 0
+
+
+@pytest.mark.parametrize("w", [4, 5, 6])
+def test_bits_word_lengths(tmp_path, monkeypatch, w):
+    data = gsdr.synth_fasta(0, n_reads=2000, seed=42)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 64, "bits", w=w)
+    assert st.k == w and st.word_index == 2
+
+
+@pytest.mark.parametrize("t", [0.88, 0.93, 0.97])
+def test_bits_thresholds(tmp_path, monkeypatch, t):
+    data = gsdr.synth_fasta(0, n_reads=2000, seed=43)
+    st, ost = run_form(data, tmp_path, monkeypatch, t, 128, "bits")
+    assert st.k == ost.k
+    if st.k <= 6:
+        assert st.word_index == 2
+
+
+def test_bits_same_pairs_as_tables(tmp_path, monkeypatch):
+    data = gsdr.synth_fasta(1, n_reads=6000, seed=44)
+    sb, _ = run_form(data, tmp_path, monkeypatch, 0.95, 256, "bits")
+    stt, _ = run_form(data, tmp_path, monkeypatch, 0.95, 256, "table")
+    assert sb.word_index == 2 and stt.word_index == 0
+    assert sb.pairs_prefilter == stt.pairs_prefilter
+    assert sb.pairs_word == stt.pairs_word
+    assert sb.pairs_aligned == stt.pairs_aligned
+    assert sb.cells == stt.cells
