@@ -2,20 +2,28 @@
 (lognormal lengths, median 1500 bp, 40k seeds, t = 0.95) on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config 1] [--batch R]
+                    [--config 1] [--reads N] [--batch R] [--no-cpu]
+                    [--plain-steps K] [--serving-jobs J] [--stage-run]
 
 One step = one full clustering of the workload (preparation kernels + every
 round).  Prints one JSON line.
   value      sequences/s with the reads already in HBM (gsdr_job_run, CUDA
-             events on the job's stream);
+             events on the job's stream), batched form;
   e2e        sequences/s through gsdr_cluster with host buffers (H2D of the
              sequence bytes and D2H of the cluster array inside the timing);
-  roofline   the filter stage (dominant HBM stream) from a stage-timed run;
+  plain      the one-representative-per-round form on the same reads, and
+             the batched / plain ratio;
+  serving    a Poisson stream of jobs through gsdr_server: p50 / p99 job
+             latency and aggregate sequences/s;
+  roofline   the filter stage (HBM) and align_roofline the alignment stage
+             (integer ALU, GCUPS) from a stage-timed run;
   cpu_baseline  the oracle (CPU restatement of the reference path) on the
              host cores, on the same workload.
 --impl reference times the oracle alone (the reference has no CPU path of its
-own) and prints its line.  Under torchrun each rank clusters an independent
-replica (the path keeps one GPU per job), rank 0 prints.
+own) and prints its line.  --stage-run runs one stage-timed clustering only
+(with GSDR_TRACE=1 a line per pass on stderr): the run the ncu captures in
+profiles/ use.  Under torchrun each rank clusters an independent replica (the
+path keeps one GPU per job), rank 0 prints.
 """
 import argparse
 import json
@@ -132,25 +140,29 @@ def key_figures():
 
 
 def filter_roofline(r, figures):
-    """The filter stage against HBM: algorithmic bytes (each candidate's
-    (k-mer, count) list once per launch) over the stage's event-timed launch
-    durations; traffic = the ncu DRAM bytes per algorithmic byte of the same
-    kernel scaled to this run's bytes per launch."""
+    """The filter stage against HBM: its input bytes (each remaining
+    candidate's k-mer list, or bitmap, plus 28 bytes, once per launch) over
+    the stage's event-timed launch durations; traffic = ncu's DRAM bytes per
+    input byte for the same kernel on this workload (profiles/), scaled to
+    this run's bytes per launch."""
     launches = max(1, r["filter_launches"])
     per_launch = r["filter_bytes"] / launches
     achieved = r["filter_gbs"]
-    key = "filter_index" if r["word_index"] else "filter_table"
-    ratio = figures.get("%s.dram_over_algorithmic" % key)
-    return {"bound": "hbm",
-            "kernel": "k_bfilter_idx (inverted k-mer index)" if r["word_index"]
-            else "k_bfilter / k_filter (k-mer tables)",
+    form = {0: "table", 1: "index", 2: "bits"}.get(r["word_index"], "table")
+    kernel = {"table": "k_bfilter (per-tentative k-mer tables in shared memory)",
+              "index": "k_bindex + k_bfilter_idx (inverted k-mer index in shared memory)",
+              "bits": "k_bfilter_bits + k_bexact (k-mer presence bitmaps)"}[form]
+    ratio = figures.get("c%d.filter_%s.dram_over_input" % (r["config"], form))
+    return {"bound": "hbm", "kernel": kernel,
             "achieved": achieved, "peak": r["peak"], "unit": "GB/s",
             "frac": achieved / r["peak"] if r["peak"] else None,
             "peak_source": r["peak_kind"] + " (MEASURED_PEAKS.json hbm_gbs)"
             if r["peak_kind"] == "measured" else r["peak_kind"],
             "traffic": per_launch * ratio if isinstance(ratio, float) else None,
-            "algorithmic_bytes_per_launch": per_launch, "launches": launches,
-            "stage_ms": r["filter_ms"]}
+            "input_bytes_per_launch": per_launch, "launches": launches,
+            "stage_ms": r["filter_ms"],
+            "note": "batched: R tentatives are tested per streamed byte, so the stage is "
+                    "bound by shared-memory lookups / popcounts, not by HBM"}
 
 
 def align_roofline(r, figures):
@@ -186,6 +198,79 @@ def write_workload(cfg, n_reads, seed, path):
     if n < 0:
         raise RuntimeError("workload generation failed")
     return n
+
+
+SERVING_T = (0.80, 0.85, 0.90, 0.95, 1.00)
+
+
+def serving_run(args, device):
+    """A Poisson stream of clustering jobs through gsdr_server (continuous
+    batching, admission by device footprint): the serving workload's recipe
+    (jobs of the 10k-read recipe with lengths 150-5000 bp, threshold drawn from
+    0.80 .. 1.00) scaled so the stream takes seconds: sizes log-uniform over
+    1k-20k reads, and 300-1.5k reads with lengths up to 2,000 bp for the
+    alignment-only thresholds (t <= 0.879 turns the filters off, which makes a
+    job quadratic in its size).  t = 1.00 jobs are rejected as the reference
+    rejects them.  Job FASTA bytes are generated before the clock starts."""
+    import gsdr
+    import numpy as np
+
+    rng = np.random.default_rng(20261207)
+    jobs = []
+    for i in range(args.serving_jobs):
+        t = float(SERVING_T[rng.integers(0, len(SERVING_T))])
+        drop = t < 0.88
+        lo, hi = (300, 1500) if drop else (1000, 20000)
+        n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        data = gsdr.synth_fasta(4, n_reads=n, seed=5000 + i, n_seeds=max(1, n // 5),
+                                len_lo=150, len_hi=2000 if drop else 5000)
+        jobs.append((data, t, n))
+    gaps = rng.exponential(1.0 / args.serving_rate, len(jobs))
+    srv = gsdr.Server(device=device, max_inflight=4)
+    lat, reads, status = {}, {}, {}
+    t0 = time.perf_counter()
+    ids = []
+    try:
+        due = t0
+        for (data, t, n), g in zip(jobs, gaps):
+            due += g
+            while True:
+                now = time.perf_counter()
+                if now >= due:
+                    break
+                r = srv.wait(int((due - now) * 1000) + 1)
+                if r:
+                    lat[r[0]], status[r[0]] = r[2], r[1]
+            jid = srv.submit(data, t)
+            ids.append(jid)
+            reads[jid] = n
+        while len(lat) < len(ids):
+            r = srv.wait(600000)
+            if r is None:
+                break
+            lat[r[0]], status[r[0]] = r[2], r[1]
+        t_end = time.perf_counter()
+        for jid in ids:
+            if jid in lat:
+                srv.release(jid)
+    finally:
+        srv.close()
+    ok = [j for j in ids if status.get(j) == 0]
+    ls = np.array([lat[j] for j in ok]) if ok else np.array([0.0])
+    done_reads = sum(reads[j] for j in ok)
+    return {
+        "jobs": len(ids), "completed": len(ok),
+        "rejected_t1": sum(1 for j in ids if status.get(j) == 1),
+        "failed": sum(1 for j in ids if status.get(j) not in (0, 1)),
+        "arrival_rate_per_s": args.serving_rate,
+        "p50_latency_ms": float(np.percentile(ls, 50)),
+        "p99_latency_ms": float(np.percentile(ls, 99)),
+        "seqs_per_s": done_reads / (t_end - t0), "reads": done_reads,
+        "wall_s": t_end - t0, "max_inflight": 4,
+        "recipe": "Poisson arrivals; jobs of the 10k-read recipe, 150-5000 bp, t in "
+                  "{0.80,0.85,0.90,0.95,1.00}; sizes 1k-20k reads (300-1.5k, <= 2000 bp "
+                  "for t <= 0.879)",
+    }
 
 
 def bench_reference(args, rank, world):
@@ -275,6 +360,8 @@ def bench_ours(args, rank, world, local):
                  "same": bool((pj.cluster() == cl_dev).all())}
         pj.close()
 
+    serving = serving_run(args, device) if args.serving_jobs > 0 else None
+
     # stage-timed run for the roofline (events around each filter / align launch)
     st_t = gsdr.clustering(f, gsdr.default_opts(threshold=t, device=device, batch=args.batch,
                                                 stage_timing=1), stats=True)[1]
@@ -293,7 +380,8 @@ def bench_ours(args, rank, world, local):
         "filter_gbs": filt_gbs, "filter_ms": st_t.ms_filter, "filter_bytes": st_t.filter_bytes,
         "filter_launches": st_t.passes if args.batch != 1 else st_t.rounds, "align_ms": st_t.ms_align, "gcups": align_gcups,
         "peak": peak, "peak_kind": peak_kind, "t": t, "plain": plain,
-        "word_index": st_t.word_index, "r_max": st_t.batch,
+        "word_index": st_t.word_index, "r_max": st_t.batch, "config": args.config,
+        "serving": serving,
     }
 
 
@@ -308,6 +396,13 @@ def main():
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--batch", type=int, default=0, help="0 = batched, adaptive R up to 256; 1 = plain")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--serving-jobs", type=int, default=40,
+                    help="jobs in the serving stream (p50/p99 latency); 0 = skip")
+    ap.add_argument("--serving-rate", type=float, default=20.0, help="job arrivals per second")
+    ap.add_argument("--stage-run", action="store_true",
+                    help="one stage-timed clustering of the workload (CUDA events around "
+                         "every filter and alignment launch; with GSDR_TRACE=1 a line per "
+                         "pass on stderr), stats as JSON: the run the ncu captures use")
     ap.add_argument("--plain-steps", type=int, default=None,
                     help="timed runs of the plain form for the batched/plain ratio "
                          "(default 2 for the 10k and 200k workloads, else 0)")
@@ -331,6 +426,17 @@ def main():
     import __graft_entry__
 
     __graft_entry__.build()
+    if args.stage_run:
+        import gsdr
+
+        f = gsdr.Fasta.parse(gsdr.synth_fasta(args.config, args.reads, args.seed))
+        _, st = gsdr.clustering(f, gsdr.default_opts(threshold=CONFIG_T[args.config],
+                                                     batch=args.batch, stage_timing=1),
+                                stats=True)
+        f.close()
+        print(json.dumps({"stage_run": CONFIG_NAMES[args.config], "batch": args.batch,
+                          "stats": st.as_dict()}), flush=True)
+        return
     if world > 1:
         dist.barrier()
     r = bench_ours(args, rank, world, local)
@@ -370,6 +476,7 @@ def main():
         "align_roofline": align_roofline(r, figures),
         "dominant_kernel": figures.get("c%d.dominant_kernel" % args.config),
         "plain": plain_line,
+        "serving": r["serving"],
         "stats": {k: r["stats"][k] for k in ("rounds", "passes", "pairs_prefilter", "pairs_word",
                                                "pairs_aligned", "pairs_accepted", "ms_prep",
                                                "ms_cluster", "word_index", "batch")},

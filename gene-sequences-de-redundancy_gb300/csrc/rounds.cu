@@ -102,6 +102,15 @@ __device__ __forceinline__ void push_pair(RoundState* st, Pair* pairs, int seg_c
     else st->pair_overflow = 1;
 }
 
+// Input bytes of the filter stage, counted once per launch for every
+// remaining candidate (filter_bytes): its composition, cutoffs and index
+// (28 bytes) and its (k-mer, count) list, or its k-mer bitmap in the bitmap
+// form.  Re-reads of the same bytes by other tentative groups are not counted.
+constexpr unsigned long long kCandFixedBytes = 16 + 8 + 4;
+__device__ __forceinline__ unsigned long long cand_bytes(const DevReads& R, int q, bool drop) {
+    return kCandFixedBytes + (drop ? 0ull : 4ull * (unsigned)R.n_kmer[q]);
+}
+
 // ---------------------------------------------------------------- plain form
 
 template <int K, bool DROP>
@@ -143,6 +152,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
         const int q = remain[idx];
         if (q == rep) continue;
         n_pf++;
+        bytes += cand_bytes(R, q, DROP);
         // kernel_preFilter (func.cu:738-754); lossless, so also used in drop mode.
         if (!prefilter_pass(crep, R.comp[q], R.cut_base[q])) continue;
         if (!DROP) {
@@ -162,7 +172,6 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
                         __popc(cb.w & rb.w);
                 }
                 d = warp_sum_i(d);
-                bytes += 4ull * NBW;
                 if (d >= cw) decided = pass = true;
                 else if (d + min(R.kextra[q], rep_extra) < cw) decided = true;
             }
@@ -178,7 +187,6 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
                     sum += min((uint32_t)table[v.z >> 16], v.z & 0xffffu);
                     sum += min((uint32_t)table[v.w >> 16], v.w & 0xffffu);
                 }
-                bytes += 16ull * ne4;
                 sum = warp_sum_i(sum);
                 pass = !(sum < cw);
             }
@@ -706,6 +714,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundSta
         const int lo = part * per, hi = min(n, lo + per);
         for (int idx = lo + (threadIdx.x >> 5); idx < hi; idx += kFilterThreads / 32) {
             const int q = remain[idx];
+            if (g == 0) bytes += cand_bytes(R, q, DROP);  // once per launch
             // lane t evaluates tentative t: order and composition bound
             bool ok = false;
             if (lane < ng) {
@@ -733,7 +742,6 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundSta
                             if (mask & (1u << t)) sum[t] += min((uint32_t)tab[t * NB + km], c);
                     }
                 }
-                bytes += 16ull * ne4;
                 const int cw = R.cut_word[q];
                 unsigned pass_mask = 0;
 #pragma unroll
@@ -820,6 +828,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter_bits(DevReads R, Rou
         const int lo = part * per, hi = min(n, lo + per);
         for (int idx = lo + warp; idx < hi; idx += WARPS) {
             const int q = remain[idx];
+            if (g == 0) bytes += kCandFixedBytes + 16ull * NQ;  // once per launch
             const int4 cq = R.comp[q];
             const int cbq = R.cut_base[q];
             unsigned ok_bits[RG / 32];
@@ -835,7 +844,6 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter_bits(DevReads R, Rou
             }
             if (!any) continue;
             for (int i = lane; i < NQ; i += 32) cb[warp][i] = __ldcs(kb4 + (size_t)q * NQ + i);
-            bytes += 16ull * NQ;
             __syncwarp();
             const int cw = R.cut_word[q];
             const int exq = R.kextra[q];
@@ -893,7 +901,6 @@ __global__ void __launch_bounds__(kFilterThreads) k_bexact(DevReads R, RoundStat
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint16_t* tab = xtab + warp * NB;
     unsigned n_al = 0;
-    unsigned long long bytes = 0;
     for (int k = blockIdx.x * WARPS + warp; k < na; k += gridDim.x * WARPS) {
         const Pair p = amb[k];
         uint4* t4 = reinterpret_cast<uint4*>(tab);
@@ -914,7 +921,6 @@ __global__ void __launch_bounds__(kFilterThreads) k_bexact(DevReads R, RoundStat
             const uint32_t v = __ldg(eq + i);
             sum += min((uint32_t)tab[v >> 16], v & 0xffffu);
         }
-        bytes += 4ull * (unsigned)(nt_ + nq);
         sum = warp_sum_i(sum);
         if (!(sum < R.cut_word[p.cand])) {
             if (lane == 0) push_pair(st, pairs, seg_cap, R, p.rep, p.cand, kBandMaxW);
@@ -922,10 +928,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_bexact(DevReads R, RoundStat
         }
         __syncwarp();
     }
-    if (lane == 0) {
-        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
-        if (bytes) atomicAdd(&st->filter_bytes, bytes);
-    }
+    if (lane == 0 && n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
 }
 
 // ---- word filter by inverted index (sparse k-mer spaces) -------------------
@@ -1108,10 +1111,8 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
             else hi = mid;
         }
         const int ntq = lo;
-        if (ntq > 0) {
-            n_pf += ntq;
-            bytes += 4ull * (unsigned)ne;
-        }
+        n_pf += ntq;
+        bytes += kCandFixedBytes + 4ull * (unsigned)ne;
         // sum over q's k-mers of min(count in q, count in tentative), per
         // tentative.  The warp takes 32 k-mers at a time, one per lane, and
         // lays their tentative lists end to end (a prefix sum of the list

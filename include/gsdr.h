@@ -71,7 +71,10 @@ typedef struct {
     int64_t pairs_aligned;    /* pairs that reached the alignment */
     int64_t pairs_accepted;
     double cells;             /* sum over aligned pairs of gap-free q x T (full-DP cells) */
-    double filter_bytes;      /* bytes the filter stage streamed (algorithmic) */
+    double filter_bytes;      /* input bytes of the filter stage: per launch, each remaining
+                                 candidate's (k-mer, count) list (word_index = 2: its k-mer
+                                 bitmap) and its 28 bytes of composition, cutoffs and
+                                 index, once (re-reads by other tentatives not counted) */
     double ms_h2d, ms_prep, ms_cluster, ms_d2h, ms_total;
     double ms_filter, ms_align; /* with stage_timing only */
     int32_t k, drop, pigeon, batch;
