@@ -70,6 +70,9 @@ struct Plan {
     int64_t idx_cap = 0;    // > 0: batched word filter by inverted index, postings capacity
     bool idx_smem = false;  // that index fits the filter's shared memory (16-bit copy)
     bool bits = false;      // batched word filter by k-mer presence bitmaps
+    // pigeon filter (p 1): low 16 bits of each read's offset in the
+    // reference's padded layout (copyData, func.cu:119-137: L/16*16 + 16 per read)
+    std::vector<uint16_t> refoff16;
 };
 
 constexpr int kSmemOptin = 227 * 1024;  // per-block shared memory limit of sm_100 / sm_103
@@ -113,6 +116,14 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
         if (ents > ents_max) ents_max = ents;
         if (i < kMaxBatch) head.push_back(head.back() + ents);
         P.kmer_off[i + 1] = P.kmer_off[i] + round4(ents);
+    }
+    if (o.pigeon == 1 && !drop) {
+        P.refoff16.resize(n);
+        int64_t ro = 0;
+        for (int i = 0; i < n; i++) {
+            P.refoff16[i] = (uint16_t)ro;
+            ro += (int64_t)reads->length[i] / 16 * 16 + 16;
+        }
     }
     if (o.batch != 1 && !drop && n > 0) {
         bool index = ents_sum * kIndexDensity <= kcap * (int64_t)n;
@@ -193,6 +204,12 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     B.idx_off16 = P.idx_smem ? c.take<uint16_t>(((size_t)1 << (2 * k)) + 8) : nullptr;
     B.idx_post16 = P.idx_smem ? c.take<uint16_t>((size_t)P.idx_cap + 8) : nullptr;
     B.amb = P.bits ? c.take<Pair>((size_t)B.seg_cap) : nullptr;
+    const bool pig = !P.refoff16.empty();
+    R.pig = pig ? c.take<uint16_t>((size_t)n * 256) : nullptr;
+    R.pidx = pig ? c.take<uint16_t>((size_t)n_bytes + 8) : nullptr;
+    R.refoff16 = pig ? c.take<uint16_t>(n) : nullptr;
+    R.pig_cap = pig ? 4 * B.seg_cap : 0;
+    R.pig_q = pig ? c.take<Pair>((size_t)R.pig_cap) : nullptr;
     return c.used + 256;
 }
 
@@ -206,8 +223,6 @@ int validate(const gsdr_reads* reads, const gsdr_opts* opts_in, gsdr_opts& o) {
     if (rc) return rc;
     if (o.drop == 0 && o.word_length > 7)
         return fail(GSDR_EUNSUPPORTED, "word length above 7 is not built yet");
-    if (o.pigeon == 1 && o.drop == 0)
-        return fail(GSDR_EUNSUPPORTED, "the pigeon filter is not built yet");
     return GSDR_OK;
 }
 
@@ -277,6 +292,8 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     carve_all(reinterpret_cast<char*>(dmem_), n, n_bytes_, P, opts.drop == 1, opts.word_length,
               R_, B_);
     stats.word_index = P.idx_cap > 0 ? 1 : (P.bits ? 2 : 0);
+    R_.threshold = opts.threshold;
+    refoff16_.swap(P.refoff16);
     pack_off_.swap(P.pack_off);
     kmer_off_.swap(P.kmer_off);
     return GSDR_OK;
@@ -295,6 +312,9 @@ int Job::upload(const gsdr_reads* reads) {
                           cudaMemcpyHostToDevice, stream));
     JCUDA(cudaMemcpyAsync((void*)R_.kmer_off, kmer_off_.data(), sizeof(int64_t) * (n + 1),
                           cudaMemcpyHostToDevice, stream));
+    if (R_.refoff16)
+        JCUDA(cudaMemcpyAsync((void*)R_.refoff16, refoff16_.data(), sizeof(uint16_t) * n,
+                              cudaMemcpyHostToDevice, stream));
     JCUDA(cudaEventRecord(ev_[1], stream));
     JCUDA(cudaStreamSynchronize(stream));  // host buffers may be released after upload
     float ms = 0;
@@ -396,6 +416,11 @@ int Job::run() {
     launch_pack(R_, opts.threshold, k, stream);
     launch_planes(R_, stream);
     stats.kernel_launches += 2;
+    if (R_.pig) {
+        // createPigeon (func.cu:252-270)
+        launch_pigeon_index(R_, stream);
+        stats.kernel_launches += 1;
+    }
     JCUDA(cudaGetLastError());
     // createWords + sortWords + mergeWords (func.cu:405-653)
     if (!drop) {
@@ -428,7 +453,7 @@ int Job::run() {
     stats.passes = h.passes;
     stats.pairs_prefilter = (int64_t)h.cnt_prefilter;
     stats.pairs_word = (int64_t)h.cnt_word;
-    stats.pairs_aligned = (int64_t)h.cnt_aligned;
+    stats.pairs_aligned = (int64_t)(h.cnt_aligned - h.cnt_pig_reject);
     stats.pairs_accepted = (int64_t)h.cnt_accepted;
     stats.cells = (double)h.cells;
     stats.filter_bytes = (double)h.filter_bytes;

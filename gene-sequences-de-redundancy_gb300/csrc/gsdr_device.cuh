@@ -28,6 +28,11 @@ constexpr int kMaxBatch = 1024;         // tentative representatives per batched
 constexpr int kTTWords = kMaxBatch / 32;
 constexpr int kMaxBitsK = 6;            // k-mer presence bitmaps for k <= 6 (4^k bits per read)
 
+struct Pair {
+    int32_t rep;   // read index of the representative (or tentative)
+    int32_t cand;  // read index of the candidate
+};
+
 struct DevReads {
     int32_t n;
     int32_t k;
@@ -53,6 +58,17 @@ struct DevReads {
     // multiplicity excess sum(count) - #distinct over those k-mers
     uint32_t* kbits;
     int32_t* kextra;
+    // pigeon filter (p 1; null otherwise), the reference's 4-mer position
+    // index: pig[256 i + v] = inclusive prefix of read i's 4-mer bucket counts
+    // (u16), pidx[off[i] + slot] = (u16) absolute position of a window's last
+    // base in the reference's padded layout, positions descending within a
+    // bucket; refoff16[i] = that layout's offset of read i (low 16 bits).
+    uint16_t* pig;
+    uint16_t* pidx;
+    const uint16_t* refoff16;
+    Pair* pig_q;        // pairs that passed the other filters, for the pigeon filter
+    int32_t pig_cap;
+    float threshold;
 };
 
 // Per-job round state, in device memory; kernels read their work sizes here so
@@ -77,16 +93,13 @@ struct RoundState {
     int32_t survivors;  // representatives confirmed this pass
     int32_t absorbed;   // reads absorbed this pass
     int32_t n_amb;      // pairs the bitmap bound left to the exact word filter
+    int32_t n_pig;      // pairs queued for the pigeon filter
     long long rounds;   // representatives taken so far
     long long passes;
     unsigned long long cnt_prefilter, cnt_word, cnt_aligned, cnt_accepted;
+    unsigned long long cnt_pig_reject;  // pairs the pigeon filter removed
     unsigned long long cells;
     unsigned long long filter_bytes;
-};
-
-struct Pair {
-    int32_t rep;   // read index of the representative (or tentative)
-    int32_t cand;  // read index of the candidate
 };
 
 // ---- prep.cu ----
@@ -96,6 +109,8 @@ void launch_pack(const DevReads& R, float t, int k, cudaStream_t s);
 int launch_kmers(const DevReads& R, int k, cudaStream_t s);
 // Base bit-planes of every read (after launch_pack).
 void launch_planes(const DevReads& R, cudaStream_t s);
+// The pigeon filter's 4-mer position index of every read (p 1).
+void launch_pigeon_index(const DevReads& R, cudaStream_t s);
 int num_sms();
 
 // ---- rounds.cu ----

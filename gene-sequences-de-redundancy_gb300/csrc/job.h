@@ -48,6 +48,7 @@ private:
     int r_max_ = 1;
     int64_t n_bytes_ = 0;
     std::vector<int64_t> pack_off_, kmer_off_;
+    std::vector<uint16_t> refoff16_;  // pigeon filter: padded-layout offsets (low 16 bits)
     void* dmem_ = nullptr;
     size_t dbytes_ = 0;
     int32_t* h_done_ = nullptr;

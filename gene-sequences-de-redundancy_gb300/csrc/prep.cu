@@ -279,12 +279,106 @@ __global__ void k_planes(DevReads R) {
     }
 }
 
+// kernel_createPigeon1 / kernel_createPigeon2 (cuda-version/func.cu:188-250)
+// for every read, one warp per read.  Over the raw codes (before the gap-free
+// packing), every position p >= 3 whose window p-3..p holds four A/C/G/T
+// bases adds one to bucket v = its 4-mer (first base most significant); pig
+// receives the inclusive prefix of the bucket counts (u16).  Within a bucket
+// the reference fills slots from the top down as p ascends, so the r-th
+// window (0-based, ascending p) of bucket v takes slot pig[v] - 1 - r; it
+// stores the window's last position in the reference's padded layout,
+// truncated to 16 bits.  Ranks within a 32-position chunk come from
+// __match_any_sync, across chunks from running per-bucket counts.
+constexpr int kPigWarps = 8;
+
+__global__ void __launch_bounds__(kPigWarps * 32) k_pigeon_index(DevReads R) {
+    __shared__ uint32_t cnt[kPigWarps][256];
+    __shared__ uint32_t run[kPigWarps][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const int nwarps = gridDim.x * kPigWarps;
+    uint32_t* c = cnt[warp];
+    uint32_t* rn = run[warp];
+    for (int r = blockIdx.x * kPigWarps + warp; r < R.n; r += nwarps) {
+        const int L = R.len[r];
+        const uint8_t* b = R.bytes + R.off[r];
+        for (int i = lane; i < 256; i += 32) {
+            c[i] = 0u;
+            rn[i] = 0u;
+        }
+        __syncwarp();
+        // bucket of the window ending at p, or -1
+        auto window = [&](int p) -> int {
+            if (p < 3 || p >= L) return -1;
+            int v = 0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int code = base_code(b[p - 3 + j]);
+                if (code > 3) return -1;
+                v = (v << 2) | code;
+            }
+            return v;
+        };
+        for (int p0 = 0; p0 < L; p0 += 32) {
+            const int v = window(p0 + lane);
+            if (v >= 0) atomicAdd(&c[v], 1u);
+        }
+        __syncwarp();
+        // inclusive prefix over the 256 buckets: lane owns 8 consecutive ones
+        uint32_t loc[8], sum = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            sum += c[lane * 8 + j];
+            loc[j] = sum;
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += o;
+        }
+        const uint32_t before = incl - sum;
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint32_t e = before + loc[j];
+            c[lane * 8 + j] = e;
+            R.pig[(size_t)r * 256 + lane * 8 + j] = (uint16_t)e;
+        }
+        __syncwarp();
+        const uint32_t base16 = R.refoff16[r];
+        uint16_t* out = R.pidx + R.off[r];
+        for (int p0 = 0; p0 < L; p0 += 32) {
+            const int p = p0 + lane;
+            const int v = window(p);
+            // invalid lanes get keys of their own
+            const unsigned grp = __match_any_sync(0xffffffffu, v >= 0 ? v : 256 + lane);
+            if (v >= 0) {
+                const uint32_t rank = rn[v] + __popc(grp & lt);
+                const uint32_t slot = c[v] - 1u - rank;
+                out[slot] = (uint16_t)(base16 + (uint32_t)p);
+            }
+            __syncwarp();
+            if (v >= 0 && (grp & lt) == 0) rn[v] += __popc(grp);
+            __syncwarp();
+        }
+    }
+}
+
 void launch_planes(const DevReads& R, cudaStream_t s) {
     if (R.n <= 0) return;
     int grid = (R.n + 7) / 8;
     const int cap = num_sms() * 16;
     if (grid > cap) grid = cap;
     k_planes<<<grid, 256, 0, s>>>(R);
+}
+
+void launch_pigeon_index(const DevReads& R, cudaStream_t s) {
+    if (R.n <= 0 || !R.pig) return;
+    int grid = (R.n + kPigWarps - 1) / kPigWarps;
+    const int cap = num_sms() * 8;
+    if (grid > cap) grid = cap;
+    k_pigeon_index<<<grid, kPigWarps * 32, 0, s>>>(R);
 }
 
 void launch_pack(const DevReads& R, float t, int k, cudaStream_t s) {

@@ -94,12 +94,28 @@ __device__ __forceinline__ int pair_class(int T, int q, int c, int band_max_w) {
     return align_class((q + 31) >> 5);
 }
 
-__device__ __forceinline__ void push_pair(RoundState* st, Pair* pairs, int seg_cap,
-                                          const DevReads& R, int rep, int q, int band_max_w) {
+__device__ __forceinline__ void queue_align(RoundState* st, Pair* pairs, int seg_cap,
+                                            const DevReads& R, int rep, int q, int band_max_w) {
     const int cls = pair_class(R.len_gf[rep], R.len_gf[q], R.cut_base[q], band_max_w);
     const int slot = atomicAdd(&st->n_pairs[cls], 1);
     if (slot < seg_cap) pairs[(size_t)cls * seg_cap + slot] = Pair{rep, q};
     else st->pair_overflow = 1;
+}
+
+// A pair that passed the composition bound and the word filter: to the
+// alignment queues, or with the pigeon filter on (p 1) to its queue first.
+// The reference applies the pigeon filter between the two (func.cu:1030-1044);
+// all three are pure functions of the pair, so the order does not change
+// which pairs reach the alignment.
+__device__ __forceinline__ void push_pair(RoundState* st, Pair* pairs, int seg_cap,
+                                          const DevReads& R, int rep, int q, int band_max_w) {
+    if (R.pig_q) {
+        const int slot = atomicAdd(&st->n_pig, 1);
+        if (slot < R.pig_cap) R.pig_q[slot] = Pair{rep, q};
+        else st->pair_overflow = 1;
+        return;
+    }
+    queue_align(st, pairs, seg_cap, R, rep, q, band_max_w);
 }
 
 // Input bytes of the filter stage, counted once per launch for every
@@ -201,6 +217,59 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
         if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
         if (bytes) atomicAdd(&st->filter_bytes, bytes);
     }
+}
+
+// kernel_pigeon (cuda-version/func.cu:756-801) on the queued pairs, one warp
+// per pair, lane = 8 of the 256 buckets: within a bucket the two position
+// lists (descending) are walked together; a pair of positions at least
+// `gap` apart counts and both lists advance, otherwise the larger position
+// advances.  gap = raw length of the representative - ceil(raw length of
+// the candidate * t), in float as the reference computes it; the pair passes
+// when the count reaches the candidate's pigeon cutoff.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_pigeon(DevReads R, RoundState* st, Pair* pairs,
+                                                int seg_cap) {
+    if (st->done) return;
+    if (BATCH && st->n_tent == 0) return;
+    const int np = min(st->n_pig, R.pig_cap);
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    unsigned rejected = 0;
+    for (int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < np; k += nwarps) {
+        const Pair p = R.pig_q[k];
+        const float prod = ceilf(__fmul_rn((float)R.len[p.cand], R.threshold));
+        const int gap = (int)__fsub_rn((float)R.len[p.rep], prod);
+        const uint16_t* pr = R.pig + (size_t)p.rep * 256;
+        const uint16_t* pc = R.pig + (size_t)p.cand * 256;
+        const uint16_t* ir = R.pidx + R.off[p.rep];
+        const uint16_t* ic = R.pidx + R.off[p.cand];
+        int sum = 0;
+        for (int t = lane; t < 256; t += 32) {
+            int s1 = t > 0 ? pr[t - 1] : 0, s2 = t > 0 ? pc[t - 1] : 0;
+            const int e1 = pr[t], e2 = pc[t];
+            while (s1 < e1 && s2 < e2) {
+                const int one = ir[s1], two = ic[s2];
+                if (abs(one - two) >= gap) {
+                    s1++;
+                    s2++;
+                    sum++;
+                } else if (one > two) {
+                    s1++;
+                } else {
+                    s2++;
+                }
+            }
+        }
+        sum = warp_sum_i(sum);
+        if (!(sum < R.cut_pig[p.cand])) {
+            if (lane == 0)
+                queue_align(st, pairs, seg_cap, R, p.rep, p.cand,
+                            BATCH ? kBandMaxW : kPlainBandMaxW);
+        } else {
+            rejected++;
+        }
+    }
+    if (lane == 0 && rejected) atomicAdd(&st->cnt_pig_reject, (unsigned long long)rejected);
 }
 
 // Decisions that need no alignment; -1 when the LCS must be computed.
@@ -565,6 +634,7 @@ __global__ void k_compact(RoundState* st, const int32_t* __restrict__ remain_in,
 }
 
 __device__ void reset_align_counters(RoundState* st, int* align_work) {
+    st->n_pig = 0;
     for (int c = 0; c < kAlignClasses; c++) {
         st->n_pairs[c] = 0;
         align_work[c] = 0;
@@ -1583,13 +1653,14 @@ void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity
     int32_t* rout = B.remain[parity ^ 1];
     if (ev4) cudaEventRecord(ev4[0], s);
     launch_filter_any<false>(R, B, rin, drop, s);
+    if (R.pig_q && !drop) k_pigeon<false><<<num_sms() * 8, 256, 0, s>>>(R, B.st, B.pairs, B.seg_cap);
     if (ev4) cudaEventRecord(ev4[1], s);
     launch_align_classes<false>(R, B, s);
     if (ev4) cudaEventRecord(ev4[2], s);
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 4 + align_launches<false>();
+    if (count) *count += 4 + align_launches<false>() + (R.pig_q && !drop ? 1 : 0);
 }
 
 void launch_align_stage(const DevReads& R, RoundBuffers& B, bool batched_mapping, bool greedy,
@@ -1611,6 +1682,7 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
                                  align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[0], s);
     launch_filter_any<true>(R, B, rin, drop, s);
+    if (R.pig_q && !drop) k_pigeon<true><<<num_sms() * 8, 256, 0, s>>>(R, B.st, B.pairs, B.seg_cap);
     if (ev4) cudaEventRecord(ev4[1], s);
     launch_align_classes<true>(R, B, s);
     if (ev4) cudaEventRecord(ev4[2], s);
@@ -1621,7 +1693,9 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 8 + align_launches<true>() + (!drop && (B.idx_off || B.amb) ? 1 : 0);
+    if (count)
+        *count += 8 + align_launches<true>() + (!drop && (B.idx_off || B.amb) ? 1 : 0) +
+                  (R.pig_q && !drop ? 1 : 0);
 }
 
 // Whether a job's per-pass k-mer index (at most `cap` postings) is kept in

@@ -63,6 +63,11 @@ CASES = {
     "edge_mixed_t95": (("fn", "edge"), ["t", "0.95"]),
     "edge_mixed_t90": (("fn", "edge"), ["t", "0.90"]),
     "ref_result_t95": (("fn", "refres"), ["t", "0.95"]),
+    # the pigeon filter (p 1)
+    "c0_3k_t95_p1": (("synth", 0, 3000, 8), ["t", "0.95", "p", "1"]),
+    "c0_2k_t90_p1": (("synth", 0, 2000, 9), ["t", "0.90", "p", "1"]),
+    "c4_2k_t93_p1": (("synth", 4, 2000, 42), ["t", "0.93", "p", "1"]),
+    "edge_mixed_t95_p1": (("fn", "edge"), ["t", "0.95", "p", "1"]),
 }
 
 

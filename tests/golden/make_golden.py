@@ -6,7 +6,10 @@ tests/golden/reference_outputs.json (or the path given as argument).
 
     oracle/build_ref.sh stage        # where the reference tree is mounted
     oracle/build_ref.sh build        # on the GPU machine
-    python tests/golden/make_golden.py [out.json]
+    python tests/golden/make_golden.py [out.json] [case ...]
+
+With case names, only those cases run and their entries are merged into the
+existing output file.
 """
 import hashlib
 import json
@@ -42,9 +45,15 @@ def main():
     import oracle_binding
 
     out_path = sys.argv[1] if len(sys.argv) > 1 else os.path.join(HERE, "reference_outputs.json")
+    only = sys.argv[2:]
     result = {}
+    if only and os.path.exists(out_path):
+        with open(out_path) as f:
+            result = json.load(f)
     with tempfile.TemporaryDirectory() as td:
         for name, (spec, argv) in cases.CASES.items():
+            if only and name not in only:
+                continue
             data = cases.build_input(spec)
             inp = os.path.join(td, name + ".fa")
             with open(inp, "wb") as f:
@@ -61,7 +70,7 @@ def main():
             opts = dict(zip(argv[0::2], argv[1::2]))
             oout = outp + ".oracle"
             oracle_binding.run(inp, oout, t=float(opts.get("t", 0.95)), w=int(opts.get("w", 0)),
-                               d=int(opts.get("d", 3)))
+                               d=int(opts.get("d", 3)), p=int(opts.get("p", 0)))
             with open(oout, "rb") as f:
                 orc_out = f.read()
             result[name] = {

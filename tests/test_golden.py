@@ -26,7 +26,8 @@ with open(os.path.join(HERE, "golden", "reference_outputs.json")) as f:
 # cases small enough for the oracle in the CPU suite
 CPU_CASES = ["c0_10k_t95", "c0_3k_t90", "c0_3k_t97", "c0_2k_t88", "c0_2k_w7",
              "c0_800_t85_drop", "c0_800_t95_d1", "c2_30k_t90", "ties_150bp_t95",
-             "edge_mixed_t95", "edge_mixed_t90", "ref_result_t95"]
+             "edge_mixed_t95", "edge_mixed_t90", "ref_result_t95", "c0_3k_t95_p1",
+             "c0_2k_t90_p1", "c4_2k_t93_p1", "edge_mixed_t95_p1"]
 
 
 def sha(b):
@@ -56,7 +57,8 @@ def test_reference_result_fasta_is_a_fixed_point():
 def test_oracle_reproduces_reference(tmp_path, name):
     data, o = case_input(name)
     _, _, _, out = orc.run_bytes(data, tmp_path, t=float(o.get("t", 0.95)),
-                                 w=int(o.get("w", 0)), d=int(o.get("d", 3)))
+                                 w=int(o.get("w", 0)), d=int(o.get("d", 3)),
+                                 p=int(o.get("p", 0)))
     assert sha(out) == GOLDEN[name]["output_sha256"]
 
 
@@ -69,7 +71,8 @@ def test_gpu_reproduces_reference(name, batch):
     try:
         cl = gsdr.clustering(f, gsdr.default_opts(threshold=float(o.get("t", 0.95)),
                                                   word_length=int(o.get("w", 0)),
-                                                  drop=int(o.get("d", 3)), batch=batch))
+                                                  drop=int(o.get("d", 3)),
+                                                  pigeon=int(o.get("p", 0)), batch=batch))
         out = f.format(cl)
     finally:
         f.close()
