@@ -550,7 +550,22 @@ int gsdr_main(int argc, char** argv) {
     const double t0 = now_ms();
     gsdr_opts o;
     std::vector<char> in(4096), out(4096);
-    if (gsdr_check_option(argc, argv, &o, in.data(), out.data(), (int64_t)in.size()) != GSDR_OK) {
+    // extension: "c <path>" also writes the cluster membership (.clstr text);
+    // the other words go to checkOption unchanged
+    std::string clstr;
+    std::vector<char*> args;
+    for (int i = 0; i < argc; i++) {
+        const char* key = argv[i];
+        while (i > 0 && i % 2 == 1 && *key == '-') key++;
+        if (i > 0 && i % 2 == 1 && key[0] == 'c' && i + 1 < argc) {
+            clstr = argv[i + 1];
+            i++;
+            continue;
+        }
+        args.push_back(argv[i]);
+    }
+    if (gsdr_check_option((int)args.size(), args.data(), &o, in.data(), out.data(),
+                          (int64_t)in.size()) != GSDR_OK) {
         std::printf("Please check parameters.\n%s\n", gsdr_last_error());
         std::printf("cluster i inputFile o outputFile t threshold [w wordLength] [d 0|1] [p 0|1]\n");
         return 0;
@@ -579,6 +594,7 @@ int gsdr_main(int argc, char** argv) {
     }
     int64_t written = 0;
     rc = gsdr_fasta_write(out.data(), f, cl.data(), &written);
+    if (!rc && !clstr.empty()) rc = gsdr_fasta_write_clusters(clstr.c_str(), f, cl.data(), nullptr);
     gsdr_fasta_free(f);
     if (rc) {
         std::printf("error: %s (%s)\n", gsdr_strerror(rc), gsdr_last_error());

@@ -215,6 +215,70 @@ int gsdr_fasta_format(const gsdr_fasta* f, const int32_t* cluster, char* buf, in
     return GSDR_OK;
 }
 
+// Cluster membership as text (no counterpart in the reference, which keeps
+// cluster[] in memory): clusters numbered in output order, members in sorted
+// order, the representative first and marked '*'.
+static int clusters_text(const gsdr_fasta* f, const int32_t* cluster, std::vector<char>& out,
+                         int64_t* n_clusters) {
+    const int32_t n = (int32_t)f->order.size();
+    std::vector<int32_t> cid(n, -1), start(n + 1, 0), member(n);
+    int32_t k = 0;
+    for (int32_t i = 0; i < n; i++) {
+        const int32_t c = cluster[i];
+        if (c < 0 || c > i || cluster[c] != c)
+            return gsdr::fail(GSDR_EINVAL, "cluster array: not a finished clustering");
+        if (c == i) cid[i] = k++;
+    }
+    for (int32_t i = 0; i < n; i++) start[cid[cluster[i]] + 1]++;
+    for (int32_t c = 0; c < k; c++) start[c + 1] += start[c];
+    std::vector<int32_t> fill(start.begin(), start.end() - 1);
+    for (int32_t i = 0; i < n; i++) member[fill[cid[cluster[i]]]++] = i;
+    const char* b = f->buf.data();
+    char num[64];
+    for (int32_t c = 0; c < k; c++) {
+        int len = std::snprintf(num, sizeof(num), ">Cluster %d\n", c);
+        out.insert(out.end(), num, num + len);
+        for (int32_t m = start[c]; m < start[c + 1]; m++) {
+            const int32_t i = member[m];
+            const int32_t r = f->order[i];
+            len = std::snprintf(num, sizeof(num), "%d\t%lldnt, ", m - start[c],
+                                (long long)f->data_len[r]);
+            out.insert(out.end(), num, num + len);
+            out.insert(out.end(), b + f->name_off[r], b + f->name_off[r] + f->name_len[r]);
+            const char* tail = cluster[i] == i ? "... *\n" : "...\n";
+            out.insert(out.end(), tail, tail + std::strlen(tail));
+        }
+    }
+    if (n_clusters) *n_clusters = k;
+    return GSDR_OK;
+}
+
+int gsdr_fasta_format_clusters(const gsdr_fasta* f, const int32_t* cluster, char* buf,
+                               int64_t cap, int64_t* need) {
+    if (!f || !cluster) return gsdr::fail(GSDR_EINVAL, "null argument");
+    std::vector<char> out;
+    const int rc = clusters_text(f, cluster, out, nullptr);
+    if (rc) return rc;
+    if (need) *need = (int64_t)out.size();
+    if (!buf) return GSDR_OK;
+    if (cap < (int64_t)out.size()) return gsdr::fail(GSDR_EINVAL, "buffer too small");
+    std::memcpy(buf, out.data(), out.size());
+    return GSDR_OK;
+}
+
+int gsdr_fasta_write_clusters(const char* path, const gsdr_fasta* f, const int32_t* cluster,
+                              int64_t* n_clusters) {
+    if (!f || !cluster || !path) return gsdr::fail(GSDR_EINVAL, "null argument");
+    std::vector<char> out;
+    const int rc = clusters_text(f, cluster, out, n_clusters);
+    if (rc) return rc;
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return gsdr::fail(GSDR_EIO, "cannot open cluster file");
+    const bool ok = std::fwrite(out.data(), 1, out.size(), fp) == out.size();
+    if (std::fclose(fp) != 0 || !ok) return gsdr::fail(GSDR_EIO, "cannot write cluster file");
+    return GSDR_OK;
+}
+
 int gsdr_fasta_write(const char* path, const gsdr_fasta* f, const int32_t* cluster,
                      int64_t* n_written) {
     if (!f || !cluster || !path) return GSDR_EINVAL;

@@ -138,6 +138,9 @@ def lib():
         L.gsdr_fasta_format.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                         P(C.c_int64)]
         L.gsdr_fasta_free.argtypes = [C.c_void_p]
+        L.gsdr_fasta_format_clusters.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                                 P(C.c_int64)]
+        L.gsdr_fasta_write_clusters.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, P(C.c_int64)]
         L.gsdr_default_opts.argtypes = [P(Opts)]
         L.gsdr_resolve_opts.argtypes = [P(Opts), P(C.c_char_p)]
         L.gsdr_check_option.argtypes = [C.c_int, P(C.c_char_p), P(Opts), C.c_char_p,
@@ -265,6 +268,23 @@ class Fasta:
         _check(lib().gsdr_fasta_write(os.fsencode(path), self._h, cl.ctypes.data, C.byref(n)))
         return n.value
 
+    def format_clusters(self, cluster: np.ndarray) -> bytes:
+        """Cluster membership text (.clstr, include/gsdr.h)."""
+        cl = np.ascontiguousarray(cluster, dtype=np.int32)
+        need = C.c_int64()
+        _check(lib().gsdr_fasta_format_clusters(self._h, cl.ctypes.data, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(max(need.value, 1))
+        _check(lib().gsdr_fasta_format_clusters(self._h, cl.ctypes.data, buf, need.value,
+                                                C.byref(need)))
+        return buf.raw[: need.value]
+
+    def write_clusters(self, path, cluster: np.ndarray) -> int:
+        cl = np.ascontiguousarray(cluster, dtype=np.int32)
+        n = C.c_int64()
+        _check(lib().gsdr_fasta_write_clusters(os.fsencode(path), self._h, cl.ctypes.data,
+                                               C.byref(n)))
+        return n.value
+
     def close(self):
         if self._h:
             lib().gsdr_fasta_free(self._h)
@@ -285,6 +305,11 @@ def read_file(path) -> Fasta:
 def save_file(path, fasta: Fasta, cluster) -> int:
     """saveFile (cuda-version/func.cu:1099-1111); returns the cluster count."""
     return fasta.write(path, cluster)
+
+
+def save_clusters(path, fasta: Fasta, cluster) -> int:
+    """Cluster membership (.clstr text, include/gsdr.h); returns the cluster count."""
+    return fasta.write_clusters(path, cluster)
 
 
 # ---- clustering ----------------------------------------------------------------

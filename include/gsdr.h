@@ -123,6 +123,20 @@ int gsdr_fasta_format(const gsdr_fasta* f, const int32_t* cluster, char* buf, in
                       int64_t* need);
 void gsdr_fasta_free(gsdr_fasta* f);
 
+/* Cluster membership (no counterpart in the reference, which keeps cluster[]
+ * in memory only; the FASTA output is unaffected), CD-HIT-like text:
+ *   >Cluster <k>                      clusters numbered in output-FASTA order
+ *   <m>\t<length>nt, <name line>... *  the representative (m = 0)
+ *   <m>\t<length>nt, <name line>...    each member, in sorted order
+ * <length> is the raw sequence length in bytes, <name line> the header with
+ * its '>'.  No identity is printed: the decision LCS >= cutoff does not compute
+ * one.  GSDR_EINVAL unless cluster[] is a finished clustering (cluster[i] <= i
+ * and cluster[cluster[i]] == cluster[i]). */
+int gsdr_fasta_format_clusters(const gsdr_fasta* f, const int32_t* cluster, char* buf,
+                               int64_t cap, int64_t* need);
+int gsdr_fasta_write_clusters(const char* path, const gsdr_fasta* f, const int32_t* cluster,
+                              int64_t* n_clusters);
+
 /* The clustering path (cuda-version/func.cu:119-653 preparation and the loop
  * of func.cu:1001-1097).  cluster[i] receives the representative of sorted
  * read i (cluster[i] == i for representatives).  Host buffers in and out;

@@ -91,3 +91,12 @@ def test_cli_reproduces_reference(tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert sha(outp.read_bytes()) == GOLDEN["c0_3k_t90"]["output_sha256"]
+    # the membership extension (c <path>) leaves the FASTA bytes unchanged
+    clstr = tmp_path / "out.clstr"
+    r = subprocess.run([gsdr.CLI_PATH, "i", str(inp), "o", str(outp), "t", o["t"],
+                        "c", str(clstr)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert sha(outp.read_bytes()) == GOLDEN["c0_3k_t90"]["output_sha256"]
+    text = clstr.read_bytes().decode()
+    assert text.count(">Cluster ") == GOLDEN["c0_3k_t90"]["records"]
+    assert text.count("\n") == text.count(">Cluster ") + len(data.split(b">")) - 1

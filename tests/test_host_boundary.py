@@ -82,3 +82,62 @@ def test_check_option_matches(argv):
 def test_dash_spelling_accepted():
     o, i, out = gsdr.check_option(["-t", "0.9", "--i", "x.fa", "-o", "y.fa"])
     assert abs(o.threshold - 0.9) < 1e-7 and i == "x.fa" and out == "y.fa" and o.word_length == 7
+
+
+# ---- cluster membership (.clstr) ----------------------------------------------
+
+def _clusters_case(tmp_path):
+    data = gsdr.synth_fasta(0, n_reads=400, seed=77)
+    _, ocl, _, ofa = orc.run_bytes(data, tmp_path, t=0.95)
+    return data, ocl, ofa
+
+
+def test_clstr_lists_every_read_once(tmp_path):
+    data, ocl, ofa = _clusters_case(tmp_path)
+    f = gsdr.Fasta.parse(data)
+    try:
+        text = f.format_clusters(ocl)
+        lens = f.lengths()
+    finally:
+        f.close()
+    lines = text.decode().splitlines()
+    heads = [l for l in lines if l.startswith(">Cluster ")]
+    reps = [l for l in lines if l.endswith("... *")]
+    members = [l for l in lines if not l.startswith(">Cluster ")]
+    assert len(heads) == len(reps) == int((ocl == np.arange(len(ocl))).sum())
+    assert len(members) == len(ocl)
+    # representatives in output order: the same names as the FASTA output
+    out_names = [l for l in ofa.decode().split("\n") if l.startswith(">")]
+    rep_names = [l.split("nt, ", 1)[1][: -len("... *")] for l in reps]
+    assert rep_names == out_names
+    # lengths are the raw sequence lengths, members of a cluster in sorted order
+    assert sorted(int(l.split("\t")[1].split("nt")[0]) for l in members) == sorted(lens.tolist())
+    for k, h in enumerate(heads):
+        assert h == f">Cluster {k}"
+
+
+def test_clstr_rejects_unfinished_clustering(tmp_path):
+    data, ocl, _ = _clusters_case(tmp_path)
+    f = gsdr.Fasta.parse(data)
+    try:
+        bad = ocl.copy()
+        bad[-1] = len(bad) + 5
+        with pytest.raises(gsdr.GsdrError):
+            f.format_clusters(bad)
+        bad = ocl.copy()
+        bad[1] = -1
+        with pytest.raises(gsdr.GsdrError):
+            f.format_clusters(bad)
+    finally:
+        f.close()
+
+
+def test_clstr_file_matches_format(tmp_path):
+    data, ocl, _ = _clusters_case(tmp_path)
+    f = gsdr.Fasta.parse(data)
+    try:
+        n = gsdr.save_clusters(str(tmp_path / "o.clstr"), f, ocl)
+        assert (tmp_path / "o.clstr").read_bytes() == f.format_clusters(ocl)
+        assert n == int((ocl == np.arange(len(ocl))).sum())
+    finally:
+        f.close()
