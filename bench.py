@@ -273,6 +273,22 @@ def serving_run(args, device):
     }
 
 
+def combine_ranks(r, world):
+    """Replicas: every rank clustered its own copy of the workload; the job's
+    time per step is the slowest rank's (max over ranks, gloo), so value =
+    all ranks' reads / that time.  Rank 0 then prints."""
+    if world <= 1:
+        return r
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([r["ms_step"], r["e2e_ms"]], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    r["ms_step"], r["e2e_ms"] = float(t[0]), float(t[1])
+    dist.barrier()
+    return r
+
+
 def bench_reference(args, rank, world):
     """--impl reference: the oracle (CPU restatement) on the host cores."""
     if rank != 0:
@@ -440,13 +456,7 @@ def main():
     if world > 1:
         dist.barrier()
     r = bench_ours(args, rank, world, local)
-    if world > 1:
-        import torch
-
-        t = torch.tensor([r["ms_step"], r["e2e_ms"]], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        r["ms_step"], r["e2e_ms"] = float(t[0]), float(t[1])
-        dist.barrier()
+    combine_ranks(r, world)
     if rank != 0:
         return
     n_total = r["n"] * world
