@@ -9,8 +9,11 @@ One step = one full clustering of the workload (preparation kernels + every
 round).  Prints one JSON line.
   value      sequences/s with the reads already in HBM (gsdr_job_run, CUDA
              events on the job's stream), batched form;
-  e2e        sequences/s through gsdr_cluster with host buffers (H2D of the
-             sequence bytes and D2H of the cluster array inside the timing);
+  e2e        sequences/s from FASTA bytes in host memory to output FASTA bytes
+             in host memory (gsdr_cluster_fasta: H2D of the file, device
+             parse, host std::sort, clustering, device formatting, D2H of the
+             output inside the timing); e2e.pre_parsed: gsdr_cluster on reads
+             parsed by the host reader;
   plain      the one-representative-per-round form on the same reads, and
              the batched / plain ratio;
   serving    a Poisson stream of jobs through gsdr_server: p50 / p99 job
@@ -282,9 +285,11 @@ def combine_ranks(r, world):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([r["ms_step"], r["e2e_ms"]], dtype=torch.float64)
+    keys = [k for k in ("ms_step", "e2e_ms", "reads_ms") if k in r]
+    t = torch.tensor([r[k] for k in keys], dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    r["ms_step"], r["e2e_ms"] = float(t[0]), float(t[1])
+    for i, k in enumerate(keys):
+        r[k] = float(t[i])
     dist.barrier()
     return r
 
@@ -352,15 +357,26 @@ def bench_ours(args, rank, world, local):
     cl_dev = job.cluster()
     job.close()
 
-    # e2e: host buffers through gsdr_cluster
+    # e2e: FASTA bytes in host memory to output FASTA bytes in host memory
+    # through gsdr_cluster_fasta (parse on the device, the host std::sort,
+    # clustering, output formatting on the device; H2D of the file, D2H of
+    # the lengths, the output and the cluster array inside the timing)
     for _ in range(min(args.warmup, 2)):
-        gsdr.clustering(f, opts)
+        gsdr.cluster_fasta(data, opts)
     e2e_ms = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        cl = gsdr.clustering(f, opts)
+        out_bytes, cl, _ = gsdr.cluster_fasta(data, opts)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    same = bool((cl == cl_dev).all())
+    same = bool((cl == cl_dev).all()) and out_bytes == f.format(cl_dev)
+    # the same with pre-parsed reads (host reader) through gsdr_cluster
+    reads_ms = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        gsdr.clustering(f, opts)
+        reads_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_h2d = len(data) + n * 8 + n * 4
+    e2e_d2h = n * 4 * 3 + len(out_bytes)
 
     # the plain form (one representative per round, the reference's loop) on
     # the same device-resident reads: the batched / plain ratio
@@ -391,7 +407,8 @@ def bench_ours(args, rank, world, local):
     align_gcups = st_t.cells / (st_t.ms_align * 1e-3) / 1e9 if st_t.ms_align > 0 else 0.0
     return {
         "n": n, "ms_step": ms_step, "ms_step_max": dev_ms_max, "e2e_ms": e2e_step,
-        "h2d": h2d, "d2h": d2h, "launches_per_step": launches // max(1, args.steps),
+        "h2d": e2e_h2d, "d2h": e2e_d2h, "reads_ms": sum(reads_ms) / len(reads_ms),
+        "reads_h2d": h2d, "reads_d2h": d2h, "launches_per_step": launches // max(1, args.steps),
         "stats": last.as_dict(), "clocks": clock_info, "same": same,
         "filter_gbs": filt_gbs, "filter_ms": st_t.ms_filter, "filter_bytes": st_t.filter_bytes,
         "filter_launches": st_t.passes if args.batch != 1 else st_t.rounds, "align_ms": st_t.ms_align, "gcups": align_gcups,
@@ -479,7 +496,13 @@ def main():
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (sequence bytes + k-mer tables > 1 GB per step)"},
         "e2e": {"value": e2e, "unit": "seqs/s", "h2d_bytes_per_step": r["h2d"],
-                "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
+                "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"],
+                "path": "gsdr_cluster_fasta: FASTA bytes -> output FASTA bytes (device parse)",
+                "pre_parsed": {"value": n_total / (r["reads_ms"] * 1e-3),
+                               "ms_per_step": r["reads_ms"],
+                               "h2d_bytes_per_step": r["reads_h2d"],
+                               "d2h_bytes_per_step": r["reads_d2h"],
+                               "path": "gsdr_cluster on reads parsed by the host reader"}},
         "gpu_launches": r["launches_per_step"] * args.steps,
         "clocks": r["clocks"],
         "roofline": filter_roofline(r, figures),

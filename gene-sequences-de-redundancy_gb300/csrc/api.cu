@@ -299,11 +299,15 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     return GSDR_OK;
 }
 
-int Job::upload(const gsdr_reads* reads) {
+int Job::upload(const gsdr_reads* reads, const void* dev_bytes) {
     if (n == 0) return GSDR_OK;
     JCUDA(cudaEventRecord(ev_[0], stream));
-    JCUDA(cudaMemcpyAsync((void*)R_.bytes, reads->bytes, (size_t)reads->n_bytes,
-                          cudaMemcpyHostToDevice, stream));
+    if (dev_bytes)
+        JCUDA(cudaMemcpyAsync((void*)R_.bytes, dev_bytes, (size_t)reads->n_bytes,
+                              cudaMemcpyDeviceToDevice, stream));
+    else
+        JCUDA(cudaMemcpyAsync((void*)R_.bytes, reads->bytes, (size_t)reads->n_bytes,
+                              cudaMemcpyHostToDevice, stream));
     JCUDA(cudaMemcpyAsync((void*)R_.off, reads->offset, sizeof(int64_t) * n,
                           cudaMemcpyHostToDevice, stream));
     JCUDA(cudaMemcpyAsync((void*)R_.len, reads->length, sizeof(int32_t) * n,
@@ -573,31 +577,52 @@ int gsdr_main(int argc, char** argv) {
     o.verbose = 1;
     std::printf("input file:\t%s\noutput file:\t%s\nthreshold:\t%g\nword length:\t%d\ndrop filter\t%d\n",
                 in.data(), out.data(), (double)o.threshold, o.word_length, o.drop);
-    gsdr_fasta* f = nullptr;
-    int rc = gsdr_fasta_read(in.data(), &f);
+    // readFile: the whole file into memory (an unreadable file reads as empty,
+    // as the reference's ifstream does); parse, sort, clustering and output
+    // formatting then run on the device (gsdr_cluster_fasta)
+    std::vector<char> text;
+    if (FILE* fp = std::fopen(in.data(), "rb")) {
+        char chunk[1 << 16];
+        size_t got;
+        while ((got = std::fread(chunk, 1, sizeof(chunk), fp)) > 0)
+            text.insert(text.end(), chunk, chunk + got);
+        std::fclose(fp);
+    }
+    gsdr_result* res = nullptr;
+    gsdr_stats st;
+    int rc = gsdr_cluster_fasta(text.data(), (int64_t)text.size(), &o, &res, &st);
     if (rc) {
         std::printf("error: %s (%s)\n", gsdr_strerror(rc), gsdr_last_error());
         return 1;
     }
-    gsdr_reads v;
-    gsdr_fasta_view(f, &v);
-    if (v.n > 0)
-        std::printf("longest:\t%d\nshortest:\t%d\nreads count:\t%d\n", v.length[0],
-                    v.length[v.n - 1], v.n);
-    std::vector<int32_t> cl(v.n > 0 ? v.n : 1);
-    gsdr_stats st;
-    rc = gsdr_cluster(&v, &o, cl.data(), &st);
-    if (rc) {
-        std::printf("error: %s (%s)\n", gsdr_strerror(rc), gsdr_last_error());
-        gsdr_fasta_free(f);
-        return 1;
+    const int32_t nr = gsdr_result_count(res);
+    const int32_t* lens = gsdr_result_lengths(res);
+    if (nr > 0)
+        std::printf("longest:\t%d\nshortest:\t%d\nreads count:\t%d\n", lens[0], lens[nr - 1], nr);
+    // saveFile (func.cu:1099-1111)
+    const char* ob = nullptr;
+    int64_t on = 0;
+    gsdr_result_output(res, &ob, &on);
+    FILE* fo = std::fopen(out.data(), "wb");
+    bool ok = fo != nullptr;
+    if (fo) {
+        ok = std::fwrite(ob, 1, (size_t)on, fo) == (size_t)on;
+        ok = std::fclose(fo) == 0 && ok;
     }
     int64_t written = 0;
-    rc = gsdr_fasta_write(out.data(), f, cl.data(), &written);
-    if (!rc && !clstr.empty()) rc = gsdr_fasta_write_clusters(clstr.c_str(), f, cl.data(), nullptr);
-    gsdr_fasta_free(f);
-    if (rc) {
-        std::printf("error: %s (%s)\n", gsdr_strerror(rc), gsdr_last_error());
+    const int32_t* cl = gsdr_result_cluster(res);
+    for (int32_t i = 0; i < nr; i++) written += cl[i] == i;
+    if (ok && !clstr.empty()) {
+        // the membership text needs the names: the host reader over the same bytes
+        gsdr_fasta* f = nullptr;
+        rc = gsdr_fasta_parse(text.data(), (int64_t)text.size(), &f);
+        if (!rc) rc = gsdr_fasta_write_clusters(clstr.c_str(), f, cl, nullptr);
+        if (f) gsdr_fasta_free(f);
+        ok = rc == GSDR_OK;
+    }
+    gsdr_result_free(res);
+    if (!ok) {
+        std::printf("error: cannot write %s\n", out.data());
         return 1;
     }
     std::printf("cluster count:\t%lld\n", (long long)written);

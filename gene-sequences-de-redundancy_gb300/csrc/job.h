@@ -17,8 +17,12 @@ public:
     ~Job();
     // Validates options and sizes, allocates device memory, creates the stream.
     int init(const gsdr_reads* reads, const gsdr_opts* opts, cudaStream_t stream = nullptr);
-    // Host -> device copy of the reads (asynchronous on the job's stream).
-    int upload(const gsdr_reads* reads);
+    // Host -> device copy of the reads; with dev_bytes, the sequence bytes are
+    // copied from that device buffer instead of reads->bytes.
+    int upload(const gsdr_reads* reads, const void* dev_bytes = nullptr);
+    // Device views for kernels that follow the clustering (output formatting).
+    const DevReads& device_reads() const { return R_; }
+    const int32_t* device_cluster() const { return B_.cluster; }
     // Preparation kernels + the round loop; the cluster array stays on device.
     int run();
     // Device -> host copy of the cluster array (synchronous).

@@ -138,6 +138,14 @@ def lib():
         L.gsdr_fasta_format.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                         P(C.c_int64)]
         L.gsdr_fasta_free.argtypes = [C.c_void_p]
+        L.gsdr_cluster_fasta.argtypes = [C.c_char_p, C.c_int64, P(Opts), P(C.c_void_p),
+                                         P(Stats)]
+        L.gsdr_result_output.argtypes = [C.c_void_p, P(C.c_void_p), P(C.c_int64)]
+        L.gsdr_result_count.argtypes = [C.c_void_p]
+        for fn in ("gsdr_result_cluster", "gsdr_result_order", "gsdr_result_lengths"):
+            getattr(L, fn).argtypes = [C.c_void_p]
+            getattr(L, fn).restype = C.c_void_p
+        L.gsdr_result_free.argtypes = [C.c_void_p]
         L.gsdr_fasta_format_clusters.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                                  P(C.c_int64)]
         L.gsdr_fasta_write_clusters.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, P(C.c_int64)]
@@ -359,6 +367,34 @@ class Job:
             self.close()
         except Exception:
             pass
+
+
+def cluster_fasta(data: bytes, opts: Opts | None = None, stats: bool = False, **kw):
+    """readFile + clustering + saveFile on the device (gsdr_cluster_fasta):
+    FASTA bytes in; returns (output FASTA bytes, cluster[] in sorted order,
+    the sort permutation), and the Stats when stats=True."""
+    o = opts if opts is not None else default_opts()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    st = Stats()
+    h = C.c_void_p()
+    _check(lib().gsdr_cluster_fasta(data, len(data), C.byref(o), C.byref(h), C.byref(st)))
+    try:
+        ptr, n = C.c_void_p(), C.c_int64()
+        _check(lib().gsdr_result_output(h, C.byref(ptr), C.byref(n)))
+        out = C.string_at(ptr.value, n.value) if n.value else b""
+        cnt = lib().gsdr_result_count(h)
+
+        def arr(fn):
+            a = np.empty(cnt, dtype=np.int32)
+            if cnt:
+                C.memmove(a.ctypes.data, getattr(lib(), fn)(h), 4 * cnt)
+            return a
+
+        cl, order = arr("gsdr_result_cluster"), arr("gsdr_result_order")
+    finally:
+        lib().gsdr_result_free(h)
+    return (out, cl, order, st) if stats else (out, cl, order)
 
 
 def cluster_bytes(data: bytes, **kw) -> bytes:

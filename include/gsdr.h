@@ -144,6 +144,24 @@ int gsdr_fasta_write_clusters(const char* path, const gsdr_fasta* f, const int32
 int gsdr_cluster(const gsdr_reads* reads, const gsdr_opts* opts, int32_t* cluster,
                  gsdr_stats* stats);
 
+/* readFile + clustering + saveFile on the device for a FASTA file already in
+ * host memory (the whole reference program, cuda-version/main.cu:3-36, minus
+ * the file I/O): the bytes are copied to the device once; record boundaries
+ * (the getline rules of func.cu:94-117) are found there; only the data
+ * lengths return to the host for the same std::sort call; the representative
+ * records are formatted on the device and only they return.  The result holds
+ * the output bytes (saveFile's), the cluster array in sorted order, the sort
+ * permutation and the sorted lengths. */
+typedef struct gsdr_result gsdr_result;
+int gsdr_cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts, gsdr_result** out,
+                       gsdr_stats* stats);
+int gsdr_result_output(const gsdr_result* r, const char** data, int64_t* n);
+int32_t gsdr_result_count(const gsdr_result* r);
+const int32_t* gsdr_result_cluster(const gsdr_result* r);  /* sorted order */
+const int32_t* gsdr_result_order(const gsdr_result* r);    /* sorted -> file position */
+const int32_t* gsdr_result_lengths(const gsdr_result* r);  /* sorted order */
+void gsdr_result_free(gsdr_result* r);
+
 /* The same path in three steps, for callers that keep a job's data on the
  * device between calls (and for timing the device part alone):
  *   gsdr_job_create  copyData (func.cu:119-137): device allocation + H2D copy
