@@ -152,7 +152,8 @@ def filter_roofline(r, figures):
     per_launch = r["filter_bytes"] / launches
     achieved = r["filter_gbs"]
     form = {0: "table", 1: "index", 2: "bits"}.get(r["word_index"], "table")
-    kernel = {"table": "k_bfilter (per-tentative k-mer tables in shared memory)",
+    kernel = {"table": "k_bfilter_tab (per-tentative k-mer tables in shared memory, "
+                       "transposed, paired 16-bit min/add)",
               "index": "k_bindex + k_bfilter_idx (inverted k-mer index in shared memory)",
               "bits": "k_bfilter_bits + k_bexact (k-mer presence bitmaps)"}[form]
     ratio = figures.get("c%d.filter_%s.dram_over_input" % (r["config"], form))

@@ -723,6 +723,137 @@ __global__ void __launch_bounds__(1024) k_bselect(RoundState* st, const int32_t*
     }
 }
 
+// Per-tentative tables, transposed (k_bfilter_tab): for each k-mer the counts
+// of a group's RG tentatives lie side by side (RG u16 = RG/8 16-byte words),
+// so one candidate entry (k-mer, count c) costs RG/8 vector loads and, per
+// pair of tentatives, one paired 16-bit min against (c, c) and one paired
+// 16-bit add into the lane's sums.  A sum is at most the candidate's k-mer
+// count (< 32768), so the halves never carry into each other, and a warp-wide
+// 32-bit reduction adds both halves at once.
+template <int K>
+struct TabGroup {
+    static constexpr int RG = K <= 5 ? 32 : K == 6 ? 16 : 4;
+    static constexpr int NB = 1 << (2 * K);
+    static constexpr int smem = NB * RG * 2;  // 64 KB (k 5), 128 KB (k 6, 7)
+};
+constexpr int kTabThreads = 1024;
+
+template <int K>
+__global__ void __launch_bounds__(kTabThreads, 1) k_bfilter_tab(DevReads R, RoundState* st,
+                                                                const int32_t* __restrict__ remain,
+                                                                const int32_t* __restrict__ tent,
+                                                                Pair* pairs, int seg_cap) {
+    constexpr int RG = TabGroup<K>::RG;
+    constexpr int W = RG / 2;  // packed sums per lane
+    constexpr int WARPS = kTabThreads / 32;
+    extern __shared__ __align__(16) uint16_t tab[];  // [NB][RG]
+    __shared__ int4 tcomp[RG];
+    __shared__ int ttent[RG];
+    if (st->done || st->n_tent == 0) return;
+    const int nt = st->n_tent;
+    const int n = st->n_remain;
+    const int ngroups = (nt + RG - 1) / RG;
+    const int parts = max(1, (int)gridDim.x / ngroups);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned n_pf = 0, n_wf = 0, n_al = 0;
+    unsigned long long bytes = 0;
+    int cur_group = -1;
+    for (int item = blockIdx.x; item < ngroups * parts; item += gridDim.x) {
+        const int g = item % ngroups, part = item / ngroups;
+        const int t0 = g * RG;
+        const int ng = min(RG, nt - t0);
+        if (g != cur_group) {
+            __syncthreads();
+            if (threadIdx.x < RG) {
+                const int i = t0 + threadIdx.x;
+                ttent[threadIdx.x] = threadIdx.x < ng ? tent[i] : 0x7fffffff;
+                tcomp[threadIdx.x] = threadIdx.x < ng ? R.comp[tent[i]] : make_int4(0, 0, 0, 0);
+            }
+            uint4* t4 = reinterpret_cast<uint4*>(tab);
+            for (int i = threadIdx.x; i < TabGroup<K>::smem / 16; i += kTabThreads)
+                t4[i] = make_uint4(0u, 0u, 0u, 0u);
+            __syncthreads();
+            // kernel_makeTable (func.cu:712-723) for each tentative: order > 0 only
+            for (int t = warp; t < ng; t += WARPS) {
+                const int rep = ttent[t];
+                const uint32_t* e = R.kmer + R.kmer_off[rep];
+                const int ne = R.n_kmer[rep];
+                for (int i = lane; i < ne; i += 32) {
+                    const uint32_t v = __ldg(e + i);
+                    const uint32_t c = v & 0xffffu;
+                    if (c) tab[(v >> 16) * RG + t] = (uint16_t)c;
+                }
+            }
+            __syncthreads();
+            cur_group = g;
+        }
+        const int per = (n + parts - 1) / parts;
+        const int lo = part * per, hi = min(n, lo + per);
+        for (int idx = lo + warp; idx < hi; idx += WARPS) {
+            const int q = remain[idx];
+            if (g == 0) bytes += cand_bytes(R, q, false);  // once per launch
+            // lane t < RG: order and composition bound of tentative t
+            bool ok = false;
+            if (lane < ng) {
+                ok = ttent[lane] < q && prefilter_pass(tcomp[lane], R.comp[q], R.cut_base[q]);
+                n_pf += ttent[lane] < q;
+            }
+            const unsigned mask = __ballot_sync(kFull, ok);
+            if (!mask) continue;
+            n_wf += ok;
+            uint32_t acc[W];
+#pragma unroll
+            for (int w = 0; w < W; w++) acc[w] = 0u;
+            const int ne4 = (R.n_kmer[q] + 3) >> 2;
+            const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
+            for (int i = lane; i < ne4; i += 32) {
+                const uint4 v = __ldcs(e4 + i);
+                const uint32_t ev[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const uint32_t c = ev[e] & 0xffffu;
+                    const uint32_t cc = c | (c << 16);
+                    const uint32_t* row = reinterpret_cast<const uint32_t*>(tab + (ev[e] >> 16) * RG);
+                    if constexpr (RG >= 8) {
+#pragma unroll
+                        for (int w = 0; w < W; w += 4) {
+                            const uint4 m = *reinterpret_cast<const uint4*>(row + w);
+                            acc[w] = __vadd2(acc[w], __vminu2(m.x, cc));
+                            acc[w + 1] = __vadd2(acc[w + 1], __vminu2(m.y, cc));
+                            acc[w + 2] = __vadd2(acc[w + 2], __vminu2(m.z, cc));
+                            acc[w + 3] = __vadd2(acc[w + 3], __vminu2(m.w, cc));
+                        }
+                    } else {
+                        const uint2 m = *reinterpret_cast<const uint2*>(row);
+                        acc[0] = __vadd2(acc[0], __vminu2(m.x, cc));
+                        acc[1] = __vadd2(acc[1], __vminu2(m.y, cc));
+                    }
+                }
+            }
+            const int cw = R.cut_word[q];
+            uint32_t mine = 0;
+#pragma unroll
+            for (int w = 0; w < W; w++) {
+                const uint32_t s = __reduce_add_sync(kFull, acc[w]);
+                if ((lane >> 1) == w) mine = s;
+            }
+            const int sum = (int)((lane & 1) ? (mine >> 16) : (mine & 0xffffu));
+            const bool pass = ok && !(sum < cw);
+            if (pass) push_pair(st, pairs, seg_cap, R, ttent[lane], q, kBandMaxW);
+            n_al += pass;
+        }
+    }
+    n_pf = (unsigned)warp_sum_i((int)n_pf);
+    n_wf = (unsigned)warp_sum_i((int)n_wf);
+    n_al = (unsigned)warp_sum_i((int)n_al);
+    if (lane == 0) {
+        if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
+        if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
+        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
+        if (bytes) atomicAdd(&st->filter_bytes, bytes);
+    }
+}
+
 // Tentatives staged per CTA: RG tables of 4^K u16 in shared memory.
 template <int K>
 struct BatchGroup {
@@ -1454,8 +1585,24 @@ void launch_filter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, 
     k_filter<K, DROP><<<grid, kFilterThreads, smem, s>>>(R, B.st, remain, B.pairs, B.seg_cap);
 }
 
+template <int K>
+void launch_bfilter_tab_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
+                          cudaStream_t s) {
+    constexpr int smem = TabGroup<K>::smem;
+    static int grid = 0;
+    if (!grid) {
+        cudaFuncSetAttribute(k_bfilter_tab<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        grid = grid_for(k_bfilter_tab<K>, kTabThreads, smem, 2);
+    }
+    k_bfilter_tab<K><<<grid, kTabThreads, smem, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap);
+}
+
 template <int K, bool DROP>
 void launch_bfilter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, cudaStream_t s) {
+    if constexpr (!DROP) {
+        launch_bfilter_tab_t<K>(R, B, remain, s);
+        return;
+    }
     const int smem = DROP ? 0 : BatchGroup<K>::smem;
     static int grid = 0;
     if (!grid) {
