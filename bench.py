@@ -3,7 +3,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--config 1] [--reads N] [--batch R] [--no-cpu]
-                    [--plain-steps K] [--serving-jobs J] [--stage-run]
+                    [--plain-steps K] [--serving-jobs J] [--autotune] [--stage-run]
 
 One step = one full clustering of the workload (preparation kernels + every
 round).  Prints one JSON line.
@@ -337,6 +337,13 @@ def bench_ours(args, rank, world, local):
     f = gsdr.Fasta.parse(data)
     n = f.n
     opts = gsdr.default_opts(threshold=t, device=device, batch=args.batch)
+    tune = None
+    if args.autotune:
+        from gsdr.autotune import autotune, tuned_opts
+
+        tune = autotune(data, t, device=device)
+        if tune["best"]:
+            opts = tuned_opts(tune, t, device=device)
     h2d = f.view.n_bytes + n * 8 + n * 4 + 2 * (n + 1) * 8
     d2h = n * 4
 
@@ -415,7 +422,7 @@ def bench_ours(args, rank, world, local):
         "filter_launches": st_t.passes if args.batch != 1 else st_t.rounds, "align_ms": st_t.ms_align, "gcups": align_gcups,
         "peak": peak, "peak_kind": peak_kind, "t": t, "plain": plain,
         "word_index": st_t.word_index, "r_max": st_t.batch, "config": args.config,
-        "serving": serving,
+        "serving": serving, "autotune": tune,
     }
 
 
@@ -433,6 +440,9 @@ def main():
     ap.add_argument("--serving-jobs", type=int, default=40,
                     help="jobs in the serving stream (p50/p99 latency); 0 = skip")
     ap.add_argument("--serving-rate", type=float, default=20.0, help="job arrivals per second")
+    ap.add_argument("--autotune", action="store_true",
+                    help="choose R_max and the word filter's form by timing them on a "
+                         "sample of the workload (gsdr.autotune) before the timed runs")
     ap.add_argument("--stage-run", action="store_true",
                     help="one stage-timed clustering of the workload (CUDA events around "
                          "every filter and alignment launch; with GSDR_TRACE=1 a line per "
@@ -511,6 +521,7 @@ def main():
         "dominant_kernel": figures.get("c%d.dominant_kernel" % args.config),
         "plain": plain_line,
         "serving": r["serving"],
+        "autotune": r["autotune"],
         "stats": {k: r["stats"][k] for k in ("rounds", "passes", "pairs_prefilter", "pairs_word",
                                                "pairs_aligned", "pairs_accepted", "ms_prep",
                                                "ms_cluster", "word_index", "batch")},

@@ -77,7 +77,8 @@ struct Plan {
 
 constexpr int kSmemOptin = 227 * 1024;  // per-block shared memory limit of sm_100 / sm_103
 
-// R_max of a job: the caller's batch, or 256 for the automatic choice.
+// R_max of a job: the caller's batch, or 256 for the automatic choice (which
+// make_plan raises for the table and index forms of the word filter).
 int job_r_max(const gsdr_opts& o) {
     return o.batch == 0 ? 256 : (o.batch > kMaxBatch ? kMaxBatch : (o.batch < 1 ? 1 : o.batch));
 }
@@ -131,11 +132,22 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
         // almost none once reads hold most of the 4^k k-mers (long reads at
         // k = 6): automatic only below a quarter of the k-mer space
         bool bits = !index && k <= kMaxBitsK && ents_sum * 4 <= kcap * (int64_t)n;
-        const char* f = std::getenv("GSDR_BFILTER");
-        if (f && std::strcmp(f, "index") == 0) index = true, bits = false;
-        if (f && std::strcmp(f, "table") == 0) index = false, bits = false;
-        if (f && std::strcmp(f, "bits") == 0) index = false, bits = k <= kMaxBitsK;
+        // the caller's choice (word_filter), else GSDR_BFILTER=table|index|bits
+        int form = o.word_filter;
+        if (form == 0) {
+            const char* f = std::getenv("GSDR_BFILTER");
+            if (f && std::strcmp(f, "table") == 0) form = 1;
+            if (f && std::strcmp(f, "index") == 0) form = 2;
+            if (f && std::strcmp(f, "bits") == 0) form = 3;
+        }
+        if (form == 1) index = false, bits = false;
+        if (form == 2) index = true, bits = false;
+        if (form == 3) index = false, bits = k <= kMaxBitsK;
         P.bits = bits;
+        // automatic R with the table form: the largest R (measured fastest on
+        // the 200k-read workload by gsdr/autotune.py: 22.6 us per
+        // representative at R_max 1024 against 25.5 at 256)
+        if (o.batch == 0 && !index && !bits) P.r_max = kMaxBatch;
         if (index) {
             // a pass indexes at most R_max tentatives: for length-sorted reads
             // those hold at most the first R_max reads' entries
@@ -407,7 +419,7 @@ int Job::loop_timed() {
     return rc;
 }
 
-int Job::run() {
+int Job::run(int pass_limit) {
     if (n == 0) return GSDR_OK;
     const double t0 = now_ms();
     const int k = opts.word_length;
@@ -434,7 +446,7 @@ int Job::run() {
     }
     JCUDA(cudaEventRecord(ev_[2], stream));
     // clustering / clusteringDrop (func.cu:1001-1097)
-    init_rounds(R_, B_, batched_ ? 1 : 0, r_max_, stream);
+    init_rounds(R_, B_, batched_ ? 1 : 0, r_max_, stream, pass_limit);
     stats.kernel_launches += 1;
     JCUDA(cudaGetLastError());
     int rc = opts.stage_timing ? loop_timed() : loop_graph();
@@ -523,6 +535,13 @@ int gsdr_job_create(const gsdr_reads* reads, const gsdr_opts* opts, gsdr_job** o
 int gsdr_job_run(gsdr_job* j, gsdr_stats* stats) {
     if (!j) return fail(GSDR_EINVAL, "null job");
     int rc = j->job.run();
+    if (stats) *stats = j->job.stats;
+    return rc;
+}
+
+int gsdr_job_run_limited(gsdr_job* j, int32_t max_passes, gsdr_stats* stats) {
+    if (!j || max_passes < 1) return fail(GSDR_EINVAL, "gsdr_job_run_limited: bad argument");
+    int rc = j->job.run(max_passes);
     if (stats) *stats = j->job.stats;
     return rc;
 }

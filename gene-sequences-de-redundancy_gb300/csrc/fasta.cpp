@@ -336,6 +336,8 @@ int gsdr_resolve_opts(gsdr_opts* o, const char** msg) {
         m = "pigeon error (pigeon=0/1)";
     } else if (o->batch < 0) {
         m = "batch must be >= 0";
+    } else if (o->word_filter < 0 || o->word_filter > 3) {
+        m = "word filter form must be 0..3";
     }
     if (m) {
         if (msg) *msg = m;

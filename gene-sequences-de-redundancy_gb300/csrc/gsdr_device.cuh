@@ -94,6 +94,7 @@ struct RoundState {
     int32_t absorbed;   // reads absorbed this pass
     int32_t n_amb;      // pairs the bitmap bound left to the exact word filter
     int32_t n_pig;      // pairs queued for the pigeon filter
+    int32_t pass_limit; // > 0: stop after this many passes (timing runs; result unfinished)
     long long rounds;   // representatives taken so far
     long long passes;
     unsigned long long cnt_prefilter, cnt_word, cnt_aligned, cnt_accepted;
@@ -143,7 +144,8 @@ struct RoundBuffers {
     // another form): pairs the bound D <= S <= D + min(excess) cannot decide
     Pair* amb;           // seg_cap pairs
 };
-void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s);
+void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
+                 int pass_limit = 0);
 // One plain round (filter, align, compact, advance); `parity` picks which
 // remain buffer is the input.  `count` accumulates kernel launches; `ev4`
 // (optional) receives events around the filter and alignment stages.

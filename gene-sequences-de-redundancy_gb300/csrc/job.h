@@ -24,7 +24,9 @@ public:
     const DevReads& device_reads() const { return R_; }
     const int32_t* device_cluster() const { return B_.cluster; }
     // Preparation kernels + the round loop; the cluster array stays on device.
-    int run();
+    // pass_limit > 0 stops after that many passes or rounds (timing only: the
+    // clustering is then unfinished).
+    int run(int pass_limit = 0);
     // Device -> host copy of the cluster array (synchronous).
     int download(int32_t* cluster);
     // Testing: decisions of the alignment stage on given (pattern, text) pairs

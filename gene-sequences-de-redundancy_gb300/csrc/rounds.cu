@@ -25,7 +25,10 @@
 // joins the first surviving tentative that accepted it.  That is exactly what
 // R consecutive reference rounds produce.
 //   k_bselect     next R unclustered indices from a forward cursor
-//   k_bfilter     prefilter + word filter of (tentative group, candidate)
+//   k_bfilter_tab / k_bfilter_idx / k_bfilter_bits (+ k_bexact)
+//                 prefilter + word filter of (tentative group, candidate):
+//                 transposed per-tentative tables, an inverted k-mer index, or
+//                 k-mer presence bitmaps; k_bprefilter in drop mode
 //   k_align       as above, accepted pairs listed instead of applied
 //   k_bsurvive    survival of the tentatives in order (one warp)
 //   k_bclaim      first surviving tentative per candidate (keyed atomicMax)
@@ -662,6 +665,7 @@ __global__ void k_advance(RoundState* st, int32_t* cluster, int* align_work) {
     st->n_next = 0;
     st->next_min = 0x7fffffff;
     reset_align_counters(st, align_work);
+    if (st->pass_limit > 0 && st->passes >= st->pass_limit) st->done = 1;  // timing runs
 }
 
 // ---------------------------------------------------------------- batched form
@@ -854,31 +858,24 @@ __global__ void __launch_bounds__(kTabThreads, 1) k_bfilter_tab(DevReads R, Roun
     }
 }
 
-// Tentatives staged per CTA: RG tables of 4^K u16 in shared memory.
-template <int K>
-struct BatchGroup {
-    static constexpr int RG = K <= 4 ? 32 : K == 5 ? 24 : K == 6 ? 12 : 3;
-    static constexpr int NB = 1 << (2 * K);
-    static constexpr int smem = RG * NB * 2;
-};
-
-template <int K, bool DROP>
-__global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundState* st,
-                                                            const int32_t* __restrict__ remain,
-                                                            const int32_t* __restrict__ tent,
-                                                            Pair* pairs, int seg_cap) {
-    constexpr int RG = DROP ? 32 : BatchGroup<K>::RG;
-    constexpr int NB = BatchGroup<K>::NB;
-    extern __shared__ __align__(16) uint16_t tab[];  // [RG][NB]
-    __shared__ int4 tcomp[32];
-    __shared__ int ttent[32];
+// Drop mode, batched (clusteringDrop, func.cu:1068-1097): only the lossless
+// composition bound (kernel_preFilter, func.cu:738-754) runs before the
+// alignment.  A CTA stages 32 tentatives; one warp per candidate, lane t
+// tests tentative t.
+__global__ void __launch_bounds__(kFilterThreads) k_bprefilter(DevReads R, RoundState* st,
+                                                               const int32_t* __restrict__ remain,
+                                                               const int32_t* __restrict__ tent,
+                                                               Pair* pairs, int seg_cap) {
+    constexpr int RG = 32;
+    __shared__ int4 tcomp[RG];
+    __shared__ int ttent[RG];
     if (st->done || st->n_tent == 0) return;
     const int nt = st->n_tent;
     const int n = st->n_remain;
     const int ngroups = (nt + RG - 1) / RG;
     const int parts = max(1, (int)gridDim.x / ngroups);
     const int lane = threadIdx.x & 31;
-    unsigned n_pf = 0, n_wf = 0, n_al = 0;
+    unsigned n_pf = 0, n_al = 0;
     unsigned long long bytes = 0;
     int cur_group = -1;
     for (int item = blockIdx.x; item < ngroups * parts; item += gridDim.x) {
@@ -892,21 +889,6 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundSta
                 ttent[threadIdx.x] = threadIdx.x < ng ? tent[i] : 0x7fffffff;
                 tcomp[threadIdx.x] = threadIdx.x < ng ? R.comp[tent[i]] : make_int4(0, 0, 0, 0);
             }
-            if (!DROP) {
-                uint32_t* t32 = reinterpret_cast<uint32_t*>(tab);
-                for (int i = threadIdx.x; i < RG * NB / 2; i += blockDim.x) t32[i] = 0u;
-                __syncthreads();
-                for (int t = 0; t < ng; t++) {
-                    const int rep = ttent[t];
-                    const uint32_t* e = R.kmer + R.kmer_off[rep];
-                    const int ne = R.n_kmer[rep];
-                    for (int i = threadIdx.x; i < ne; i += blockDim.x) {
-                        const uint32_t v = __ldg(e + i);
-                        const uint32_t c = v & 0xffffu;
-                        if (c) tab[t * NB + (v >> 16)] = (uint16_t)c;
-                    }
-                }
-            }
             __syncthreads();
             cur_group = g;
         }
@@ -915,54 +897,20 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter(DevReads R, RoundSta
         const int lo = part * per, hi = min(n, lo + per);
         for (int idx = lo + (threadIdx.x >> 5); idx < hi; idx += kFilterThreads / 32) {
             const int q = remain[idx];
-            if (g == 0) bytes += cand_bytes(R, q, DROP);  // once per launch
-            // lane t evaluates tentative t: order and composition bound
+            if (g == 0) bytes += cand_bytes(R, q, true);  // once per launch
             bool ok = false;
             if (lane < ng) {
-                const int rep = ttent[lane];
-                ok = rep < q && prefilter_pass(tcomp[lane], R.comp[q], R.cut_base[q]);
+                ok = ttent[lane] < q && prefilter_pass(tcomp[lane], R.comp[q], R.cut_base[q]);
+                n_pf += ttent[lane] < q;
             }
-            unsigned mask = __ballot_sync(kFull, ok);
-            n_pf += lane < ng && ttent[lane] < q;
-            if (!mask) continue;
-            if (!DROP) {
-                n_wf += __popc(mask);
-                int sum[RG];
-#pragma unroll
-                for (int t = 0; t < RG; t++) sum[t] = 0;
-                const int ne4 = (R.n_kmer[q] + 3) >> 2;
-                const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
-                for (int i = lane; i < ne4; i += 32) {
-                    const uint4 v = __ldcs(e4 + i);
-                    const uint32_t ev[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        const uint32_t km = ev[e] >> 16, c = ev[e] & 0xffffu;
-#pragma unroll
-                        for (int t = 0; t < RG; t++)
-                            if (mask & (1u << t)) sum[t] += min((uint32_t)tab[t * NB + km], c);
-                    }
-                }
-                const int cw = R.cut_word[q];
-                unsigned pass_mask = 0;
-#pragma unroll
-                for (int t = 0; t < RG; t++) {
-                    if (mask & (1u << t)) {
-                        const int s = warp_sum_i(sum[t]);
-                        if (!(s < cw)) pass_mask |= 1u << t;
-                    }
-                }
-                mask = pass_mask;
-            }
-            if (lane < ng && (mask & (1u << lane)))
-                push_pair(st, pairs, seg_cap, R, ttent[lane], q, kBandMaxW);
-            n_al += __popc(mask);
+            if (ok) push_pair(st, pairs, seg_cap, R, ttent[lane], q, kBandMaxW);
+            n_al += ok;
         }
     }
-    n_pf = warp_sum_i((int)n_pf);
+    n_pf = (unsigned)warp_sum_i((int)n_pf);
+    n_al = (unsigned)warp_sum_i((int)n_al);
     if (lane == 0) {
         if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
-        if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
         if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
         if (bytes) atomicAdd(&st->filter_bytes, bytes);
     }
@@ -1531,10 +1479,12 @@ __global__ void k_badvance(RoundState* st, const int32_t* __restrict__ tent, int
         return;
     }
     st->n_remain = n;
+    if (st->pass_limit > 0 && st->passes >= st->pass_limit) st->done = 1;  // timing runs
 }
 
 __global__ void k_init(RoundState* st, int32_t* cluster, int32_t* remain, uint32_t* tidx,
-                       uint32_t* best, int n, int batched, int r_max, int* align_work) {
+                       uint32_t* best, int n, int batched, int r_max, int pass_limit,
+                       int* align_work) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         if (batched) {
@@ -1556,6 +1506,7 @@ __global__ void k_init(RoundState* st, int32_t* cluster, int32_t* remain, uint32
         s.pass = 1;
         s.R = 1;
         s.R_max = r_max;
+        s.pass_limit = pass_limit;
         *st = s;
         for (int c = 0; c <= kSingleWorkSlot; c++) align_work[c] = 0;
     }
@@ -1601,18 +1552,11 @@ template <int K, bool DROP>
 void launch_bfilter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, cudaStream_t s) {
     if constexpr (!DROP) {
         launch_bfilter_tab_t<K>(R, B, remain, s);
-        return;
+    } else {
+        static int grid = 0;
+        if (!grid) grid = grid_for(k_bprefilter, kFilterThreads, 0, 8);
+        k_bprefilter<<<grid, kFilterThreads, 0, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap);
     }
-    const int smem = DROP ? 0 : BatchGroup<K>::smem;
-    static int grid = 0;
-    if (!grid) {
-        if (smem > 0)
-            cudaFuncSetAttribute(k_bfilter<K, DROP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem);
-        grid = grid_for(k_bfilter<K, DROP>, kFilterThreads, smem, 8);
-    }
-    k_bfilter<K, DROP><<<grid, kFilterThreads, smem, s>>>(R, B.st, remain, B.tent, B.pairs,
-                                                          B.seg_cap);
 }
 
 template <int K>
@@ -1786,12 +1730,13 @@ void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bo
 // the same allocation.
 static int* align_work_of(RoundState* st) { return reinterpret_cast<int*>(st + 1); }
 
-void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s) {
+void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
+                 int pass_limit) {
     const int n = R.n;
     const int threads = 256;
     const int blocks = n > 0 ? (n + threads - 1) / threads : 1;
     k_init<<<blocks, threads, 0, s>>>(B.st, B.cluster, B.remain[0], B.tidx, B.best, n, batched,
-                                      r_max, align_work_of(B.st));
+                                      r_max, pass_limit, align_work_of(B.st));
 }
 
 void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,

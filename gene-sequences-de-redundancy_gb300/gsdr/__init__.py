@@ -39,6 +39,7 @@ class Opts(C.Structure):
         ("device", C.c_int32),
         ("stage_timing", C.c_int32),
         ("verbose", C.c_int32),
+        ("word_filter", C.c_int32),
     ]
 
 
@@ -146,6 +147,7 @@ def lib():
             getattr(L, fn).argtypes = [C.c_void_p]
             getattr(L, fn).restype = C.c_void_p
         L.gsdr_result_free.argtypes = [C.c_void_p]
+        L.gsdr_job_run_limited.argtypes = [C.c_void_p, C.c_int32, P(Stats)]
         L.gsdr_fasta_format_clusters.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                                  P(C.c_int64)]
         L.gsdr_fasta_write_clusters.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, P(C.c_int64)]
@@ -347,9 +349,14 @@ class Job:
         _check(lib().gsdr_job_create(C.byref(fasta.view), C.byref(opts), C.byref(h)))
         self._h = h
 
-    def run(self) -> Stats:
+    def run(self, max_passes: int = 0) -> Stats:
+        """gsdr_job_run; with max_passes > 0, gsdr_job_run_limited (timing only:
+        the clustering stops unfinished after that many passes)."""
         st = Stats()
-        _check(lib().gsdr_job_run(self._h, C.byref(st)))
+        if max_passes > 0:
+            _check(lib().gsdr_job_run_limited(self._h, max_passes, C.byref(st)))
+        else:
+            _check(lib().gsdr_job_run(self._h, C.byref(st)))
         return st
 
     def cluster(self) -> np.ndarray:

@@ -49,6 +49,9 @@ typedef struct {
     int32_t device;       /* CUDA device ordinal */
     int32_t stage_timing; /* 1: time each stage with CUDA events (slower; for profiling) */
     int32_t verbose;      /* 1: print the reference's progress lines to stdout */
+    int32_t word_filter;  /* batched word filter form: 0 automatic, 1 per-tentative k-mer
+                             tables, 2 inverted k-mer index, 3 k-mer presence bitmaps
+                             (k <= 6); the result is the same in every form */
 } gsdr_opts;
 
 /* Reads in length-sorted order (the order readFile leaves them in).  Read i is

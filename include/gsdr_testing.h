@@ -10,6 +10,8 @@
 #define GSDR_TESTING_H
 #include <stdint.h>
 
+#include "gsdr.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -24,6 +26,11 @@ extern "C" {
 int gsdr_lcs_decide(const char* bytes, int64_t n_bytes, const int64_t* off, const int32_t* len,
                     int32_t n_seq, const int32_t* pat, const int32_t* txt, int32_t n_pairs,
                     float t, int32_t mapping, int32_t greedy, uint8_t* accept, double* ms);
+
+/* gsdr_job_run (include/gsdr.h) stopped after max_passes passes (batched) or
+ * rounds (plain): the clustering is left unfinished.  For timing settings on
+ * the early, full-size passes of a job (gsdr/autotune.py). */
+int gsdr_job_run_limited(gsdr_job* job, int32_t max_passes, gsdr_stats* stats);
 
 #ifdef __cplusplus
 }

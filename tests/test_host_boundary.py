@@ -141,3 +141,23 @@ def test_clstr_file_matches_format(tmp_path):
         assert n == int((ocl == np.arange(len(ocl))).sum())
     finally:
         f.close()
+
+
+def test_autotune_sample_is_whole_records():
+    from gsdr.autotune import sample_fasta
+
+    data = gsdr.synth_fasta(0, n_reads=500, seed=3)
+    s = sample_fasta(data, 100, seed=2)
+    recs = s.split(b"\n")
+    assert s.startswith(b">") and s.endswith(b"\n")
+    assert len(recs[:-1]) == 200
+    full = set(data.split(b"\n")[1::2])
+    assert all(r in full for r in recs[1:-1:2])
+    assert sample_fasta(data, 1000) == data
+
+
+def test_word_filter_option_range():
+    o = gsdr.default_opts(word_filter=4)
+    with pytest.raises(gsdr.GsdrError):
+        gsdr.resolve_opts(o)
+    assert gsdr.resolve_opts(gsdr.default_opts(word_filter=2)).word_filter == 2
