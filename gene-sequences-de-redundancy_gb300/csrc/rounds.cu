@@ -36,7 +36,8 @@
 //   k_compact, k_badvance
 // R adapts per pass: it halves after a pass in which representatives absorbed
 // many reads (tentatives there mostly repeat each other's work) and doubles
-// otherwise, up to the caller's maximum.  The result does not depend on R.
+// otherwise (8x after a pass too small to fill the device), up to the
+// caller's maximum.  The result does not depend on R.
 #include <cuda_runtime.h>
 
 #include "gsdr_device.cuh"
@@ -51,6 +52,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kFilterThreads = 256;
 constexpr int kAlignThreads = 256;  // 8 warps: 8/G groups of G warps
 constexpr int kAbsorbHigh = 64;     // absorbed reads per representative that shrink R
+constexpr int kFewPairs = 16384;    // queued pairs below which R grows 8x, not 2x
 // Largest band window (words) sent to the banded kernel: batched passes, plain
 // rounds.  A plain round waits for its slowest pair, and a lane works through
 // its pair alone, so the plain form keeps long pairs on the systolic kernels.
@@ -1469,8 +1471,12 @@ __global__ void k_badvance(RoundState* st, const int32_t* __restrict__ tent, int
     const int nt = st->n_tent;
     if (nt > 0) st->cursor = tent[nt - 1] + 1;
     const int surv = max(1, st->survivors);
+    // a pass that queued fewer pairs than the device keeps in flight ran on
+    // the latency of its longest pairs: grow R faster
+    int queued = 0;
+    for (int c = 0; c < kAlignClasses; c++) queued += st->n_pairs[c];
     if (st->absorbed > kAbsorbHigh * surv) st->R = max(1, st->R / 2);
-    else st->R = min(st->R_max, st->R * 2);
+    else st->R = min(st->R_max, st->R * (queued < kFewPairs ? 8 : 2));
     const int n = st->n_next;
     st->n_next = 0;
     st->next_min = 0x7fffffff;
