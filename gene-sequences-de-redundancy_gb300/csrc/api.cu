@@ -283,7 +283,7 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     r_max_ = P.r_max;
     stats.batch = batched_ ? r_max_ : 1;
     if (P.max_len > 32 * kMaxPatternWords)
-        return fail(GSDR_EUNSUPPORTED, "reads above 32768 bases are not built yet");
+        return fail(GSDR_EUNSUPPORTED, "reads above 65536 bases are not built yet");
     int dev_count = 0;
     if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
         return fail(GSDR_EDEVICE, "no CUDA device");

@@ -19,8 +19,8 @@
 
 namespace gsdr {
 
-constexpr int kMaxPatternWords = 1024;  // 8 warps x 32 lanes x 4 words: 32768 gap-free bases
-constexpr int kSysClasses = 6;          // pattern length classes of the systolic alignment kernels
+constexpr int kMaxPatternWords = 2048;  // 8 warps x 32 lanes x 8 words: 65536 gap-free bases
+constexpr int kSysClasses = 7;          // pattern length classes of the systolic alignment kernels
 constexpr int kBandClasses = 4;         // window classes (4, 8, 16, 32 words) of the banded kernel
 constexpr int kAlignClasses = kSysClasses + kBandClasses;  // alignment queues
 constexpr int kSingleWorkSlot = 15;     // work counter of the merged single-warp systolic classes

@@ -30,13 +30,15 @@ namespace gsdr {
 namespace {
 
 constexpr int kNaMaxPairs = GSDR_NOALLOC_MAX_PAIRS;
+constexpr int kNaClasses = 6;      // systolic classes 0..5: patterns of at most 1024 words
+constexpr int kNaMaxWords = 1024;  // 32768 gap-free bases, the documented limit
 constexpr int kNaMaxSeqs = GSDR_NOALLOC_MAX_SEQS;
 constexpr int kNaMaxDevices = 64;
 
 // Layout of the array (offsets in bytes, each 256-aligned).
 constexpr size_t kOffState = 0;                                   // RoundState + counters
-constexpr size_t kOffPairs = 1024;                                // kSysClasses x kNaMaxPairs
-constexpr size_t kOffCut = kOffPairs + sizeof(Pair) * (size_t)kSysClasses * kNaMaxPairs;
+constexpr size_t kOffPairs = 1024;                                // kNaClasses x kNaMaxPairs
+constexpr size_t kOffCut = kOffPairs + sizeof(Pair) * (size_t)kNaClasses * kNaMaxPairs;
 constexpr size_t kOffCluster = kOffCut + sizeof(int32_t) * (size_t)kNaMaxSeqs;
 constexpr size_t kScratchBytes = kOffCluster + sizeof(int32_t) * (size_t)kNaMaxSeqs;
 static_assert(sizeof(RoundState) + 64 * sizeof(int) <= kOffPairs, "state area too small");
@@ -92,7 +94,7 @@ __global__ void k_na_bucket(RoundState* st, Pair* pairs, const int32_t* __restri
             continue;
         }
         const int words = (len_gf[p] + 31) >> 5;
-        if (words > kMaxPatternWords) {
+        if (words > kNaMaxWords) {
             st->pair_overflow = 1;
             continue;
         }

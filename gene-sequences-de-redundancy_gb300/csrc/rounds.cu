@@ -67,17 +67,17 @@ __device__ __forceinline__ bool prefilter_pass(const int4 a, const int4 b, int c
 
 // Alignment class of a pattern of `words` 32-base words; the classes hold the
 // same word counts in both forms, as warps x words per lane:
-//   class            0       1       2        3        4        5
-//   words          <=32    <=64   <=128    <=256    <=512   <=1024
-//   plain form      1x1     1x2     2x2      4x2      8x2      8x4
-//   batched form    1x1     1x2     1x4      1x8      2x8      4x8
+//   class            0       1       2        3        4        5        6
+//   words          <=32    <=64   <=128    <=256    <=512   <=1024   <=2048
+//   plain form      1x1     1x2     2x2      4x2      8x2      8x4      8x8
+//   batched form    1x1     1x2     1x4      1x8      2x8      4x8      8x8
 // The plain form waits for every round's longest pair, so it spreads a pattern
 // over more warps (shorter per-base chain); the batched form has many pairs in
 // flight and packs each pattern into as few warps as it can (fewer
 // instructions per DP cell, no hand-offs between warps).
 __device__ __forceinline__ int align_class(int words) {
     return words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 256 ? 3
-                                                             : words <= 512 ? 4 : 5;
+                         : words <= 512 ? 4 : words <= 1024 ? 5 : 6;
 }
 
 // Queue of a pair: a band class (kSysClasses + 0..3 for windows of 4, 8, 16,
@@ -734,7 +734,7 @@ __global__ void __launch_bounds__(1024) k_bselect(RoundState* st, const int32_t*
 // so one candidate entry (k-mer, count c) costs RG/8 vector loads and, per
 // pair of tentatives, one paired 16-bit min against (c, c) and one paired
 // 16-bit add into the lane's sums.  A sum is at most the candidate's k-mer
-// count (< 32768), so the halves never carry into each other, and a warp-wide
+// count (< 65536), so the halves never carry into each other, and a warp-wide
 // 32-bit reduction adds both halves at once.
 template <int K>
 struct TabGroup {
@@ -1324,7 +1324,7 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
                             ct = pp & 0xffffu;
                         }
                         // 16-bit halves cannot carry: a sum is at most the
-                        // candidate's k-mer count, below 32768
+                        // candidate's k-mer count, below 65536
                         if (t < (uint32_t)ntq)
                             atomicAdd(&acc[t >> 1], min(ct, co) << ((t & 1u) << 4));
                     }
@@ -1722,11 +1722,13 @@ void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bo
             R, B.st, align_args(B), reinterpret_cast<int*>(B.st + 1) + kSingleWorkSlot);
         launch_align_t<2, 8, BATCH>(R, B, 4, s);
         launch_align_t<4, 8, BATCH>(R, B, 5, s);
+        launch_align_t<8, 8, BATCH>(R, B, 6, s);
     } else {
         launch_align_t<2, 2, BATCH>(R, B, 2, s);
         launch_align_t<4, 2, BATCH>(R, B, 3, s);
         launch_align_t<8, 2, BATCH>(R, B, 4, s);
         launch_align_t<8, 4, BATCH>(R, B, 5, s);
+        launch_align_t<8, 8, BATCH>(R, B, 6, s);
     }
 }
 
@@ -1769,7 +1771,7 @@ void launch_align_stage(const DevReads& R, RoundBuffers& B, bool batched_mapping
 
 int align_class_host(int words) {
     return words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 256 ? 3
-                                                             : words <= 512 ? 4 : 5;
+                         : words <= 512 ? 4 : words <= 1024 ? 5 : 6;
 }
 
 void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,

@@ -134,3 +134,34 @@ def test_single_read_and_no_newline(tmp_path):
     cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95)
     assert_same(cl, ocl, out, ofa)
     assert out == b">only\nACGTACGTAC\n"
+
+
+@pytest.mark.parametrize("batch", [1, 0])
+def test_reads_above_32k_bases(tmp_path, batch):
+    # 33-65 kbp reads: patterns of the 8-warp x 8-word class (up to 65,536 bases)
+    rng = np.random.default_rng(91)
+    codes = np.frombuffer(b"ACGT", dtype=np.uint8)
+    recs = []
+    for s in range(3):
+        base = codes[rng.integers(0, 4, 65000)].tobytes()
+        for c in range(4):
+            L = int(rng.integers(33000, 65000))
+            seq = bytearray(base[:L])
+            for _ in range(int(rng.integers(0, L // 40))):
+                seq[int(rng.integers(0, L))] = int(codes[rng.integers(0, 4)])
+            recs.append(b">s%d_%d\n" % (s, c) + bytes(seq) + b"\n")
+    data = b"".join(recs)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95, batch=batch)
+    assert_same(cl, ocl, out, ofa)
+    assert st.pairs_accepted == ost.accepted
+
+
+def test_reads_above_64k_bases_are_refused():
+    data = b">a\n" + b"ACGT" * 16500 + b"\n>b\nACGT\n"
+    f = gsdr.Fasta.parse(data)
+    try:
+        with pytest.raises(gsdr.GsdrError) as e:
+            gsdr.clustering(f, gsdr.default_opts(threshold=0.95))
+        assert e.value.status == gsdr.EUNSUPPORTED
+    finally:
+        f.close()
