@@ -95,7 +95,7 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
     const int k = o.word_length;
     P.pack_off.assign(n + 1, 0);
     P.kmer_off.assign(n + 1, 0);
-    P.r_max = o.batch == 1 ? 1 : job_r_max(o);
+    P.r_max = (o.batch == 1 || (!drop && k >= kWideK)) ? 1 : job_r_max(o);
     const int64_t kcap = (int64_t)1 << (2 * (k > 0 ? k : 1));
     int64_t ents_sum = 0, ents_max = 0;
     std::vector<int64_t> head;  // entries of the first kMaxBatch reads, prefix sums
@@ -126,7 +126,7 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
             ro += (int64_t)reads->length[i] / 16 * 16 + 16;
         }
     }
-    if (o.batch != 1 && !drop && n > 0) {
+    if (o.batch != 1 && !drop && n > 0 && k < kWideK) {
         bool index = ents_sum * kIndexDensity <= kcap * (int64_t)n;
         // the bitmap bound decides almost every pair of short reads but
         // almost none once reads hold most of the 4^k k-mers (long reads at
@@ -216,6 +216,15 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     B.idx_off16 = P.idx_smem ? c.take<uint16_t>(((size_t)1 << (2 * k)) + 8) : nullptr;
     B.idx_post16 = P.idx_smem ? c.take<uint16_t>((size_t)P.idx_cap + 8) : nullptr;
     B.amb = P.bits ? c.take<Pair>((size_t)B.seg_cap) : nullptr;
+    // word lengths 8..12: k-mer ids and counts apart, the global table, the
+    // per-CTA hash scratch (slots: a power of two >= 2 x the longest read)
+    const bool wide = !drop && k >= kWideK;
+    R.kcnt = wide ? c.take<uint16_t>((size_t)P.kmer_off[n] + 8) : nullptr;
+    R.gtab = wide ? c.take<uint16_t>((size_t)1 << (2 * k)) : nullptr;
+    int slots = 1024;
+    while (wide && slots < 2 * P.max_len) slots <<= 1;
+    R.khash_slots = wide ? slots : 0;
+    R.khash = wide ? c.take<uint32_t>((size_t)kHashCtas * 3 * slots) : nullptr;
     const bool pig = !P.refoff16.empty();
     R.pig = pig ? c.take<uint16_t>((size_t)n * 256) : nullptr;
     R.pidx = pig ? c.take<uint16_t>((size_t)n_bytes + 8) : nullptr;
@@ -233,8 +242,6 @@ int validate(const gsdr_reads* reads, const gsdr_opts* opts_in, gsdr_opts& o) {
     o = *opts_in;
     int rc = gsdr_resolve_opts(&o, nullptr);
     if (rc) return rc;
-    if (o.drop == 0 && o.word_length > 7)
-        return fail(GSDR_EUNSUPPORTED, "word length above 7 is not built yet");
     return GSDR_OK;
 }
 
@@ -272,7 +279,9 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     stats.k = opts.word_length;
     stats.drop = opts.drop;
     stats.pigeon = opts.pigeon;
-    batched_ = opts.batch != 1;
+    // word lengths 8..12 run one representative per round (the batched
+    // filters keep the 4^k k-mer space on chip)
+    batched_ = opts.batch != 1 && !(opts.drop == 0 && opts.word_length >= kWideK);
     {
         const char* tr = std::getenv("GSDR_TRACE");
         trace_ = tr && tr[0] == '1';
@@ -439,6 +448,8 @@ int Job::run(int pass_limit) {
     }
     JCUDA(cudaGetLastError());
     // createWords + sortWords + mergeWords (func.cu:405-653)
+    if (R_.gtab)
+        JCUDA(cudaMemsetAsync(R_.gtab, 0, sizeof(uint16_t) * ((size_t)1 << (2 * k)), stream));
     if (!drop) {
         if (launch_kmers(R_, k, stream)) return fail(GSDR_EDEVICE, "k-mer kernel configuration");
         stats.kernel_launches += 1;

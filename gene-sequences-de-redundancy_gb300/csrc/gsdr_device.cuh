@@ -63,6 +63,15 @@ struct DevReads {
     // (u16), pidx[off[i] + slot] = (u16) absolute position of a window's last
     // base in the reference's padded layout, positions descending within a
     // bucket; refoff16[i] = that layout's offset of read i (low 16 bits).
+    // word lengths above 7 (k-mer ids wider than 16 bits): kmer holds the
+    // k-mer ids and kcnt their u16 counts (null for k <= 7); gtab is the
+    // representative's 4^k-entry count table in global memory, as the
+    // reference's (func.cu:712-736); khash is a per-CTA hash scratch for
+    // counting each read's k-mers (khash_slots slots of {key, count})
+    uint16_t* kcnt;
+    uint16_t* gtab;
+    uint32_t* khash;
+    int32_t khash_slots;
     uint16_t* pig;
     uint16_t* pidx;
     const uint16_t* refoff16;
@@ -106,8 +115,11 @@ struct RoundState {
 // ---- prep.cu ----
 // Parse + gap-free pack + composition + cutoffs, one warp per read.
 void launch_pack(const DevReads& R, float t, int k, cudaStream_t s);
-// Distinct k-mers with multiplicities for every read (k <= 7).
+// Distinct k-mers with multiplicities for every read.
 int launch_kmers(const DevReads& R, int k, cudaStream_t s);
+// CTAs of the hash-based k-mer count (k >= 8): each owns R.khash_slots slots.
+constexpr int kHashCtas = 128;
+constexpr int kWideK = 8;  // word lengths from here on use the wide k-mer layout
 // Base bit-planes of every read (after launch_pack).
 void launch_planes(const DevReads& R, cudaStream_t s);
 // The pigeon filter's 4-mer position index of every read (p 1).

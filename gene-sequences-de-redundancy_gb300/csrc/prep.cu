@@ -389,14 +389,83 @@ void launch_pack(const DevReads& R, float t, int k, cudaStream_t s) {
     k_pack<<<grid, kPackWarps * 32, 0, s>>>(R, t, k);
 }
 
+// Word lengths 8..12 (createWords / sortWords / mergeWords, func.cu:405-653):
+// the distinct k-mers of each read with their u16 multiplicities, counted in
+// an open-addressing hash table of the CTA's own (global memory, L2
+// resident).  The first thread that claims a slot records it in the CTA's
+// slot list; after the read the listed slots are emitted (ids into R.kmer,
+// counts into R.kcnt, in slot-claim order: the filters need the multiset, not
+// an order) and cleared for the next read.
+__global__ void __launch_bounds__(256) k_kmers_hash(DevReads R, int k) {
+    const int S = R.khash_slots;  // a power of two, at least 2 x the longest read
+    uint32_t* keys = R.khash + (size_t)blockIdx.x * 3 * S;
+    uint32_t* cnt = keys + S;
+    uint32_t* slots = cnt + S;
+    __shared__ int nlist;
+    const uint32_t mask = (k >= 16) ? 0xffffffffu : ((1u << (2 * k)) - 1u);
+    const int shift = 32 - (31 - __clz(S));
+    for (int r = blockIdx.x; r < R.n; r += gridDim.x) {
+        if (threadIdx.x == 0) nlist = 0;
+        __syncthreads();
+        const int nk = R.len_gf[r] - k + 1;
+        const uint32_t* pk = R.packed + R.pack_off[r];
+        for (int p = threadIdx.x; p < nk; p += blockDim.x) {
+            const int w = p >> 4, o = p & 15;
+            const uint64_t v = ((uint64_t)__ldg(pk + w) << 32) | __ldg(pk + w + 1);
+            const uint32_t km = (uint32_t)(v >> (64 - 2 * o - 2 * k)) & mask;
+            uint32_t h = (km * 0x9e3779b1u) >> shift;
+            for (int probe = 0; probe < S; probe++) {
+                const uint32_t old = atomicCAS(&keys[h], 0xffffffffu, km);
+                if (old == 0xffffffffu) slots[atomicAdd(&nlist, 1)] = h;
+                if (old == 0xffffffffu || old == km) {
+                    atomicAdd(&cnt[h], 1u);
+                    break;
+                }
+                h = (h + 1) & (uint32_t)(S - 1);
+            }
+        }
+        __syncthreads();
+        const int nl = nlist;
+        uint32_t* ok = R.kmer + R.kmer_off[r];
+        uint16_t* oc = R.kcnt + R.kmer_off[r];
+        for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+            const uint32_t h = slots[i];
+            ok[i] = keys[h];
+            oc[i] = (uint16_t)(cnt[h] & 0xffffu);  // the reference's u16 multiplicity
+            keys[h] = 0xffffffffu;
+            cnt[h] = 0u;
+        }
+        for (int i = nl + threadIdx.x; i < ((nl + 3) & ~3); i += blockDim.x) {
+            ok[i] = 0u;
+            oc[i] = 0u;
+        }
+        if (threadIdx.x == 0) R.n_kmer[r] = nl;
+        __syncthreads();
+    }
+}
+
+__global__ void k_khash_init(DevReads R) {
+    const int S = R.khash_slots;
+    const size_t total = (size_t)kHashCtas * 3 * S;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t part = (i / S) % 3;  // per CTA: keys, counts, slot list
+        R.khash[i] = part == 0 ? 0xffffffffu : 0u;
+    }
+}
+
 int launch_kmers(const DevReads& R, int k, cudaStream_t s) {
     if (R.n <= 0) return 0;
+    if (k >= kWideK && R.khash) k_khash_init<<<num_sms() * 4, 256, 0, s>>>(R);
     switch (k) {
         case 4: return kmers_hist_launch<4>(R, s);
         case 5: return kmers_hist_launch<5>(R, s);
         case 6: return kmers_hist_launch<6>(R, s);
         case 7: return kmers_hist_launch<7>(R, s);
-        default: return 2;
+        default:
+            if (k < kWideK || k > 12 || !R.khash) return 2;
+            k_kmers_hash<<<kHashCtas, 256, 0, s>>>(R, k);
+            return 0;
     }
 }
 

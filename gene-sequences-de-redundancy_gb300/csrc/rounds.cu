@@ -129,7 +129,8 @@ __device__ __forceinline__ void push_pair(RoundState* st, Pair* pairs, int seg_c
 // form.  Re-reads of the same bytes by other tentative groups are not counted.
 constexpr unsigned long long kCandFixedBytes = 16 + 8 + 4;
 __device__ __forceinline__ unsigned long long cand_bytes(const DevReads& R, int q, bool drop) {
-    return kCandFixedBytes + (drop ? 0ull : 4ull * (unsigned)R.n_kmer[q]);
+    // (k >= 8: 4-byte k-mer ids and 2-byte counts)
+    return kCandFixedBytes + (drop ? 0ull : (R.kcnt ? 6ull : 4ull) * (unsigned)R.n_kmer[q]);
 }
 
 // ---------------------------------------------------------------- plain form
@@ -275,6 +276,64 @@ __global__ void __launch_bounds__(256) k_pigeon(DevReads R, RoundState* st, Pair
         }
     }
     if (lane == 0 && rejected) atomicAdd(&st->cnt_pig_reject, (unsigned long long)rejected);
+}
+
+// ---- word lengths 8..12, plain form: the reference's global table ----------
+//
+// kernel_makeTable / kernel_filter / kernel_cleanTable (func.cu:712-736,
+// 803-826): the representative's counts go into a 4^k-entry table in global
+// memory (set before the filter, cleared after it), and one warp per
+// candidate sums min(table[k-mer], count) over the candidate's entries.
+
+__global__ void k_gtab(DevReads R, RoundState* st, int clear) {
+    if (st->done) return;
+    const int rep = st->rep;
+    const uint32_t* e = R.kmer + R.kmer_off[rep];
+    const uint16_t* c = R.kcnt + R.kmer_off[rep];
+    const int ne = R.n_kmer[rep];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x) {
+        if (clear) R.gtab[e[i]] = 0;
+        else if (c[i]) R.gtab[e[i]] = c[i];  // only order > 0
+    }
+}
+
+__global__ void __launch_bounds__(kFilterThreads) k_filter_g(DevReads R, RoundState* st,
+                                                             const int32_t* __restrict__ remain,
+                                                             Pair* pairs, int seg_cap) {
+    if (st->done) return;
+    const int rep = st->rep;
+    const int n = st->n_remain;
+    if (n <= 0) return;
+    const int lane = threadIdx.x & 31;
+    const int4 crep = R.comp[rep];
+    unsigned n_pf = 0, n_wf = 0, n_al = 0;
+    unsigned long long bytes = 0;
+    const int nwarps = gridDim.x * (kFilterThreads / 32);
+    for (int idx = blockIdx.x * (kFilterThreads / 32) + (threadIdx.x >> 5); idx < n;
+         idx += nwarps) {
+        const int q = remain[idx];
+        if (q == rep) continue;
+        n_pf++;
+        bytes += cand_bytes(R, q, false);
+        if (!prefilter_pass(crep, R.comp[q], R.cut_base[q])) continue;
+        n_wf++;
+        const uint32_t* e = R.kmer + R.kmer_off[q];
+        const uint16_t* c = R.kcnt + R.kmer_off[q];
+        const int ne = R.n_kmer[q];
+        int sum = 0;
+        for (int i = lane; i < ne; i += 32)
+            sum += min((uint32_t)__ldg(R.gtab + __ldg(e + i)), (uint32_t)__ldg(c + i));
+        sum = warp_sum_i(sum);
+        if (sum < R.cut_word[q]) continue;
+        n_al++;
+        if (lane == 0) push_pair(st, pairs, seg_cap, R, rep, q, kPlainBandMaxW);
+    }
+    if (lane == 0) {
+        if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
+        if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
+        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
+        if (bytes) atomicAdd(&st->filter_bytes, bytes);
+    }
 }
 
 // Decisions that need no alignment; -1 when the LCS must be computed.
@@ -1619,6 +1678,14 @@ void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* re
 template <bool BATCH>
 void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain, int drop,
                        cudaStream_t s) {
+    if (!BATCH && !drop && R.k >= kWideK) {
+        static int grid = 0;
+        if (!grid) grid = grid_for(k_filter_g, kFilterThreads, 0, 8);
+        k_gtab<<<64, 256, 0, s>>>(R, B.st, 0);
+        k_filter_g<<<grid, kFilterThreads, 0, s>>>(R, B.st, remain, B.pairs, B.seg_cap);
+        k_gtab<<<64, 256, 0, s>>>(R, B.st, 1);
+        return;
+    }
     if (BATCH && !drop && B.amb) {
         switch (R.k) {
             case 4: launch_bfilter_bits_t<4>(R, B, remain, s); break;
@@ -1760,7 +1827,9 @@ void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
-    if (count) *count += 4 + align_launches<false>() + (R.pig_q && !drop ? 1 : 0);
+    if (count)
+        *count += 4 + align_launches<false>() + (R.pig_q && !drop ? 1 : 0) +
+                  (!drop && R.k >= kWideK ? 2 : 0);
 }
 
 void launch_align_stage(const DevReads& R, RoundBuffers& B, bool batched_mapping, bool greedy,

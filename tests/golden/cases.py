@@ -68,6 +68,10 @@ CASES = {
     "c0_2k_t90_p1": (("synth", 0, 2000, 9), ["t", "0.90", "p", "1"]),
     "c4_2k_t93_p1": (("synth", 4, 2000, 42), ["t", "0.93", "p", "1"]),
     "edge_mixed_t95_p1": (("fn", "edge"), ["t", "0.95", "p", "1"]),
+    # word lengths above 7 (w override)
+    "c0_2k_w8": (("synth", 0, 2000, 10), ["t", "0.95", "w", "8"]),
+    "c0_2k_w10": (("synth", 0, 2000, 11), ["t", "0.93", "w", "10"]),
+    "c0_1k_w12": (("synth", 0, 1000, 12), ["t", "0.95", "w", "12"]),
 }
 
 

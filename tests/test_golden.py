@@ -27,7 +27,8 @@ with open(os.path.join(HERE, "golden", "reference_outputs.json")) as f:
 CPU_CASES = ["c0_10k_t95", "c0_3k_t90", "c0_3k_t97", "c0_2k_t88", "c0_2k_w7",
              "c0_800_t85_drop", "c0_800_t95_d1", "c2_30k_t90", "ties_150bp_t95",
              "edge_mixed_t95", "edge_mixed_t90", "ref_result_t95", "c0_3k_t95_p1",
-             "c0_2k_t90_p1", "c4_2k_t93_p1", "edge_mixed_t95_p1"]
+             "c0_2k_t90_p1", "c4_2k_t93_p1", "edge_mixed_t95_p1", "c0_2k_w8",
+             "c0_2k_w10", "c0_1k_w12"]
 
 
 def sha(b):

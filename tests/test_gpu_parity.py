@@ -56,11 +56,25 @@ def test_thresholds_word_lengths(tmp_path, t):
     assert_same(cl, ocl, out, ofa)
 
 
-@pytest.mark.parametrize("w", [4, 5, 6, 7])
+@pytest.mark.parametrize("w", [4, 5, 6, 7, 8, 9, 10, 11, 12])
 def test_word_length_override(tmp_path, w):
     data = gsdr.synth_fasta(0, n_reads=1500, seed=5)
     cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.95, w=w)
     assert_same(cl, ocl, out, ofa)
+    assert st.k == w
+    assert st.pairs_word == ost.prefilter_pass
+    assert st.pairs_aligned == ost.aligned
+
+
+@pytest.mark.parametrize("w,t,p", [(8, 0.90, 0), (9, 0.95, 1), (12, 0.97, 0)])
+def test_long_word_lengths_long_reads(tmp_path, w, t, p):
+    # reads of a few thousand bases: the k-mer hash of a read takes more than
+    # its smallest table; a batched request runs one representative per round
+    data = gsdr.synth_fasta(1, n_reads=400, seed=21)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=t, w=w, p=p, batch=0)
+    assert_same(cl, ocl, out, ofa)
+    assert st.batch == 1
+    assert st.pairs_word == ost.prefilter_pass
 
 
 @pytest.mark.parametrize("t", [0.80, 0.85])
