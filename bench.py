@@ -399,6 +399,13 @@ def bench_ours(args, rank, world, local):
         plain = {"ms": sum(pms) / len(pms), "steps": len(pms),
                  "same": bool((pj.cluster() == cl_dev).all())}
         pj.close()
+        # its filter stage (one representative per launch, HBM-shaped) from a
+        # stage-timed run
+        sp = gsdr.clustering(f, gsdr.default_opts(threshold=t, device=device, batch=1,
+                                                  stage_timing=1), stats=True)[1]
+        plain["filter_ms"] = sp.ms_filter
+        plain["filter_bytes"] = sp.filter_bytes
+        plain["filter_launches"] = sp.rounds
 
     serving = serving_run(args, device) if args.serving_jobs > 0 else None
 
@@ -497,6 +504,17 @@ def main():
         plain_line = {"value": pv, "unit": "seqs/s", "ms_per_step": r["plain"]["ms"],
                       "steps": r["plain"]["steps"], "batched_over_plain": value / pv,
                       "same_clusters": r["plain"]["same"]}
+        if r["plain"].get("filter_ms"):
+            pg = r["plain"]["filter_bytes"] / (r["plain"]["filter_ms"] * 1e-3) / 1e9
+            plain_line["filter_roofline"] = {
+                "bound": "hbm", "kernel": "k_filter (one representative per launch)",
+                "achieved": pg, "peak": r["peak"], "unit": "GB/s",
+                "frac": pg / r["peak"] if r["peak"] else None,
+                "input_bytes_per_launch": r["plain"]["filter_bytes"] /
+                max(1, r["plain"]["filter_launches"]),
+                "launches": r["plain"]["filter_launches"], "stage_ms": r["plain"]["filter_ms"],
+                "note": "bytes the filter reads: 28 per remaining candidate, its k-mer list "
+                        "where the composition bound passed"}
     line = {
         "metric": "seqs/sec", "value": value, "unit": "seqs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_step"],

@@ -73,6 +73,7 @@ struct Plan {
     // pigeon filter (p 1): low 16 bits of each read's offset in the
     // reference's padded layout (copyData, func.cu:119-137: L/16*16 + 16 per read)
     std::vector<uint16_t> refoff16;
+    int variant = 0;  // gsdr_opts::variant
 };
 
 constexpr int kSmemOptin = 227 * 1024;  // per-block shared memory limit of sm_100 / sm_103
@@ -95,6 +96,7 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
     const int k = o.word_length;
     P.pack_off.assign(n + 1, 0);
     P.kmer_off.assign(n + 1, 0);
+    P.variant = o.variant;
     P.r_max = (o.batch == 1 || (!drop && k >= kWideK)) ? 1 : job_r_max(o);
     const int64_t kcap = (int64_t)1 << (2 * (k > 0 ? k : 1));
     int64_t ents_sum = 0, ents_max = 0;
@@ -190,6 +192,9 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     R.n_kmer = c.take<int32_t>(n);
     R.kmer = c.take<uint32_t>((size_t)P.kmer_off[n] + 8);
     R.bm = c.take<uint32_t>(2 * (size_t)P.pack_off[n] + 8);
+    R.variant = P.variant;
+    R.strict = P.variant == 1 ? 1 : 0;
+    R.brk = P.variant == 1 && !drop ? c.take<uint32_t>((size_t)P.pack_off[n] + 8) : nullptr;
     const bool bits = !drop && k <= kMaxBitsK;
     const size_t nbw = bits ? ((size_t)1 << (2 * k)) / 32 : 0;
     R.kbits = bits ? c.take<uint32_t>((size_t)n * nbw) : nullptr;
@@ -314,6 +319,11 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
               R_, B_);
     stats.word_index = P.idx_cap > 0 ? 1 : (P.bits ? 2 : 0);
     R_.threshold = opts.threshold;
+    R_.band_serial = kBandMaxSerial;
+    if (const char* bs = std::getenv("GSDR_BAND_SERIAL")) R_.band_serial = std::atoll(bs);
+    R_.group_max_w = kGroupMaxWords;
+    if (const char* gw = std::getenv("GSDR_GROUP_MAXW"))
+        R_.group_max_w = std::min(std::max(std::atoi(gw), 0), kGroupMaxWords);
     refoff16_.swap(P.refoff16);
     pack_off_.swap(P.pack_off);
     kmer_off_.swap(P.kmer_off);
@@ -407,16 +417,20 @@ int Job::loop_timed() {
         if (trace_) {
             // per-step trace on stderr: the state after the step
             RoundState h;
-            if (cudaMemcpy(&h, B_.st, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess)
+            if (cudaMemcpy(&h, B_.st, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess) {
+                // queues: systolic classes | lane-band classes | group-band classes
+                std::string q;
+                for (int c = 0; c < kAlignClasses; c++)
+                    q += (c == kSysClasses || c == kSysClasses + kBandClasses ? " | " : " ") +
+                         std::to_string(h.n_pairs[c]);
                 std::fprintf(stderr,
                              "gsdr trace: step %lld rounds %lld tentatives %d R %d remain %d "
                              "aligned %llu filter %.3f ms align %.3f ms filter_bytes %llu "
-                             "queues %d %d %d %d %d %d | %d %d %d %d\n",
+                             "queues%s\n",
                              (long long)h.passes, (long long)h.rounds, h.n_tent, h.R, h.n_remain,
                              (unsigned long long)h.cnt_aligned, a, b,
-                             (unsigned long long)h.filter_bytes, h.n_pairs[0], h.n_pairs[1],
-                             h.n_pairs[2], h.n_pairs[3], h.n_pairs[4], h.n_pairs[5], h.n_pairs[6],
-                             h.n_pairs[7], h.n_pairs[8], h.n_pairs[9]);
+                             (unsigned long long)h.filter_bytes, q.c_str());
+            }
         }
         parity ^= 1;
         if (*h_done_) break;
@@ -438,6 +452,8 @@ int Job::run(int pass_limit) {
     JCUDA(cudaEventRecord(ev_[1], stream));
     // baseToNumber + compressData + createCutoff + createPrefix (func.cu:139-403)
     JCUDA(cudaMemsetAsync(R_.packed, 0, sizeof(uint32_t) * ((size_t)pack_off_[n] + 8), stream));
+    if (R_.brk)
+        JCUDA(cudaMemsetAsync(R_.brk, 0, sizeof(uint32_t) * ((size_t)pack_off_[n] + 8), stream));
     launch_pack(R_, opts.threshold, k, stream);
     launch_planes(R_, stream);
     stats.kernel_launches += 2;
@@ -601,7 +617,8 @@ int gsdr_main(int argc, char** argv) {
     if (gsdr_check_option((int)args.size(), args.data(), &o, in.data(), out.data(),
                           (int64_t)in.size()) != GSDR_OK) {
         std::printf("Please check parameters.\n%s\n", gsdr_last_error());
-        std::printf("cluster i inputFile o outputFile t threshold [w wordLength] [d 0|1] [p 0|1]\n");
+        std::printf("cluster i inputFile o outputFile t threshold [w wordLength] [d 0|1] [p 0|1]"
+                    " [v 0|1] [c clusterFile]\n");
         return 0;
     }
     o.verbose = 1;
@@ -696,6 +713,13 @@ int Job::lcs_pairs(const int32_t* pat, const int32_t* txt, int n_pairs, int mapp
             if (T > 0 && cb > 0 && q >= cb && T >= cb) {
                 const int bw = band_words(T, q, cb);
                 if (bw <= 32) c = kSysClasses + (bw <= 4 ? 0 : bw <= 8 ? 1 : bw <= 16 ? 2 : 3);
+            }
+        } else if (mapping == 3) {
+            // the group-banded kernel where the band fits 128 words
+            const int T = gf[txt[k]], q = gf[pat[k]], cb = cut[pat[k]];
+            if (T > 0 && cb > 0 && q >= cb && T >= cb) {
+                const int bw = band_words(T, q, cb);
+                if (bw <= kGroupMaxWords) c = group_class(bw);
             }
         }
         cls[c].push_back(Pair{txt[k], pat[k]});

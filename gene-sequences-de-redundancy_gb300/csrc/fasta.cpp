@@ -338,10 +338,28 @@ int gsdr_resolve_opts(gsdr_opts* o, const char** msg) {
         m = "batch must be >= 0";
     } else if (o->word_filter < 0 || o->word_filter > 3) {
         m = "word filter form must be 0..3";
+    } else if (o->variant != 0 && o->variant != 1) {
+        m = "variant must be 0 (cuda-version) or 1 (SYCL program)";
+    } else if (o->variant == 1 && o->word_length != 0 &&
+               (o->word_length < 4 || o->word_length > 8)) {
+        m = "word length out of range (4<=word length<=8)";  // func.cpp:47-51
+    } else if (o->variant == 1 && (o->drop == 1 || o->pigeon != 0)) {
+        m = "the SYCL program has no drop mode and no pigeon filter";
     }
     if (m) {
         if (msg) *msg = m;
         return gsdr::fail(GSDR_EINVAL, m);
+    }
+    if (o->variant == 1) {
+        // func.cpp:36-45: the word length rises with t; filters always on
+        if (o->word_length == 0) {
+            if (o->threshold < 0.88) o->word_length = 4;
+            else if (o->threshold < 0.94) o->word_length = 5;
+            else if (o->threshold < 0.97) o->word_length = 6;
+            else o->word_length = 7;
+        }
+        o->drop = 0;
+        return GSDR_OK;
     }
     if (o->word_length == 0) {
         if (o->threshold < 0.88) o->word_length = 4;
@@ -359,6 +377,7 @@ int gsdr_check_option(int argc, char** argv, gsdr_opts* o, char* in_path, char* 
     gsdr_default_opts(o);
     std::string in = "testData.fasta", out = "result.fasta";
     if (argc % 2 != 1) return gsdr::fail(GSDR_EINVAL, "odd number of option words");
+    bool drop_key = false, pigeon_key = false;
     for (int i = 1; i < argc; i += 2) {
         const char* key = argv[i];
         while (*key == '-') key++;  // also accept -t / --t spellings
@@ -369,16 +388,19 @@ int gsdr_check_option(int argc, char** argv, gsdr_opts* o, char* in_path, char* 
                 case 'o': out = val; break;
                 case 't': o->threshold = std::stof(val); break;
                 case 'w': o->word_length = std::stoi(val); break;
-                case 'd': o->drop = std::stoi(val); break;
-                case 'p': o->pigeon = std::stoi(val); break;
+                case 'd': o->drop = std::stoi(val); drop_key = true; break;
+                case 'p': o->pigeon = std::stoi(val); pigeon_key = true; break;
                 case 'b': o->batch = std::stoi(val); break;  // extension: tentatives per pass
                 case 'g': o->device = std::stoi(val); break;  // extension: CUDA device
+                case 'v': o->variant = std::stoi(val); break;  // extension: semantics
                 default: return gsdr::fail(GSDR_EINVAL, "unknown option");
             }
         } catch (...) {
             return gsdr::fail(GSDR_EINVAL, "option value does not parse");
         }
     }
+    if (o->variant == 1 && (drop_key || pigeon_key))
+        return gsdr::fail(GSDR_EINVAL, "unknown option");  // func.cpp:27-29: usage
     if ((int64_t)in.size() + 1 > cap || (int64_t)out.size() + 1 > cap)
         return gsdr::fail(GSDR_EINVAL, "path too long");
     std::memcpy(in_path, in.c_str(), in.size() + 1);

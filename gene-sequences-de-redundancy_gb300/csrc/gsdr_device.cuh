@@ -22,8 +22,17 @@ namespace gsdr {
 constexpr int kMaxPatternWords = 2048;  // 8 warps x 32 lanes x 8 words: 65536 gap-free bases
 constexpr int kSysClasses = 7;          // pattern length classes of the systolic alignment kernels
 constexpr int kBandClasses = 4;         // window classes (4, 8, 16, 32 words) of the banded kernel
-constexpr int kAlignClasses = kSysClasses + kBandClasses;  // alignment queues
-constexpr int kSingleWorkSlot = 15;     // work counter of the merged single-warp systolic classes
+constexpr int kGroupClasses = 5;        // group-banded classes: 2, 4, 8, 16, 32 lanes x 4 words
+constexpr int kGroupMaxWords = 128;     // widest window of the group-banded kernel
+constexpr int kAlignClasses = kSysClasses + kBandClasses + kGroupClasses;  // alignment queues
+constexpr int kSingleWorkSlot = kAlignClasses;  // work counter of the merged single-warp systolic classes
+
+// Group-banded class of a window of bw <= kGroupMaxWords words: the fewest
+// lanes (2, 4, .. 32) whose 4 words each hold it.
+__host__ __device__ __forceinline__ int group_class(int bw) {
+    const int g = bw <= 8 ? 0 : bw <= 16 ? 1 : bw <= 32 ? 2 : bw <= 64 ? 3 : 4;
+    return kSysClasses + kBandClasses + g;
+}
 constexpr int kMaxBatch = 1024;         // tentative representatives per batched pass
 constexpr int kTTWords = kMaxBatch / 32;
 constexpr int kMaxBitsK = 6;            // k-mer presence bitmaps for k <= 6 (4^k bits per read)
@@ -63,6 +72,11 @@ struct DevReads {
     // (u16), pidx[off[i] + slot] = (u16) absolute position of a window's last
     // base in the reference's padded layout, positions descending within a
     // bucket; refoff16[i] = that layout's offset of read i (low 16 bits).
+    uint16_t* pig;
+    uint16_t* pidx;
+    const uint16_t* refoff16;
+    Pair* pig_q;        // pairs that passed the other filters, for the pigeon filter
+    int32_t pig_cap;
     // word lengths above 7 (k-mer ids wider than 16 bits): kmer holds the
     // k-mer ids and kcnt their u16 counts (null for k <= 7); gtab is the
     // representative's 4^k-entry count table in global memory, as the
@@ -72,11 +86,23 @@ struct DevReads {
     uint16_t* gtab;
     uint32_t* khash;
     int32_t khash_slots;
-    uint16_t* pig;
-    uint16_t* pidx;
-    const uint16_t* refoff16;
-    Pair* pig_q;        // pairs that passed the other filters, for the pigeon filter
-    int32_t pig_cap;
+    // largest serial work (text bases x window words) of a pair given to the
+    // lane-per-pair banded kernel; longer pairs go to the systolic kernels
+    int64_t band_serial;
+    // widest window (words) given to the group-banded kernel (kGroupMaxWords;
+    // 0: none, those pairs go to the systolic kernels)
+    int32_t group_max_w;
+    // semantics (gsdr_opts::variant): 1 = the SYCL program's.  brk (variant 1
+    // with filters, null otherwise): bit g of read i (word pack_off[i] + g/32)
+    // is set when a non-ACGT byte stands right before gap-free base g in the
+    // raw read; a k-mer whose window holds such a break is not a k-mer there
+    // (func.cpp:238-274 skips raw windows that hold a non-ACGT byte)
+    uint32_t* brk;
+    int32_t variant;
+    // 1 with variant 1: cut_base holds the alignment's cutoff ceil(len * t)
+    // + 1 (LCS > ceil(len * t), func.cpp:671) and the composition prefilter
+    // compares with cut_base - strict (func.cpp:532-547)
+    int32_t strict;
     float threshold;
 };
 
@@ -120,6 +146,8 @@ int launch_kmers(const DevReads& R, int k, cudaStream_t s);
 // CTAs of the hash-based k-mer count (k >= 8): each owns R.khash_slots slots.
 constexpr int kHashCtas = 128;
 constexpr int kWideK = 8;  // word lengths from here on use the wide k-mer layout
+// Default of DevReads::band_serial (GSDR_BAND_SERIAL overrides it).
+constexpr long long kBandMaxSerial = 16384;
 // Base bit-planes of every read (after launch_pack).
 void launch_planes(const DevReads& R, cudaStream_t s);
 // The pigeon filter's 4-mer position index of every read (p 1).

@@ -53,6 +53,20 @@ __device__ void cutoffs(int length, float t, int k, int* word, int* base, int* p
     *pig = (int)__dmul_rn(c1, 4.0);
 }
 
+// createCutoff of the SYCL program (func.cpp:339-373): the same formulas in
+// float, the offset forced to 1; its alignment accepts LCS > ceil(len * t)
+// (func.cpp:671), stored here as the cutoff ceil(len * t) + 1 of an LCS >=
+// test (the prefilter subtracts DevReads::strict again).
+__device__ void cutoffs_sycl(int length, float t, int k, int* word, int* base) {
+    int required = length - k + 1;
+    const float slack = ceilf(__fmul_rn((float)length, __fsub_rn(1.0f, t)));
+    const int cutoff = (int)__fmul_rn(slack, (float)k);
+    required -= cutoff;
+    required = max(required, 1);
+    *word = required;
+    *base = (int)ceilf(__fmul_rn((float)length, t)) + 1;
+}
+
 __global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, int k) {
     __shared__ uint32_t stage_all[kPackWarps][36];
     const int lane = threadIdx.x & 31;
@@ -71,6 +85,8 @@ __global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, i
         __syncwarp();
         int gcount = 0;
         int cnt0 = 0, cnt1 = 0, cnt2 = 0, cnt3 = 0;
+        uint32_t* brk = R.brk ? R.brk + R.pack_off[r] : nullptr;
+        bool gap_before = false;  // the byte before this iteration's first chunk
         for (long long c0 = 0; c0 < nchunks; c0 += 32) {
             const long long c = c0 + lane;
             uint4 v = make_uint4(0, 0, 0, 0);
@@ -78,12 +94,27 @@ __global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, i
             const uint32_t words[4] = {v.x, v.y, v.z, v.w};
             int nb = 0;
             uint32_t acc = 0;
+            uint32_t gaps = 0;   // bit jj: byte jj of the chunk is a non-ACGT byte of the read
+            uint32_t marks = 0;  // bit b: the chunk's b-th base follows a non-ACGT byte
+            uint32_t before = 0; // the byte before the chunk is one
+            if (brk) {
+                // the previous lane's last byte, or for lane 0 the last byte of
+                // the previous iteration
+                const long long p15 = 16 * c + 15 - head;
+                const bool v15 = (c < nchunks) && p15 >= 0 && p15 < L;
+                const uint32_t last_gap = v15 && base_code(words[3] >> 24) == 4 ? 1u : 0u;
+                before = __shfl_up_sync(0xffffffffu, last_gap, 1);
+                if (lane == 0) before = gap_before ? 1u : 0u;
+                gap_before = __shfl_sync(0xffffffffu, last_gap, 31) != 0;
+            }
 #pragma unroll
             for (int jj = 0; jj < 16; jj++) {
                 const long long pos = 16 * c + jj - head;
                 const bool valid = (c < nchunks) && pos >= 0 && pos < L;
                 const int code = valid ? base_code((words[jj >> 2] >> (8 * (jj & 3))) & 0xffu) : 4;
+                if (valid && code == 4) gaps |= 1u << jj;
                 if (code < 4) {
+                    if ((jj == 0 ? before : (gaps >> (jj - 1))) & 1u) marks |= 1u << nb;
                     acc = (acc << 2) | (uint32_t)code;
                     nb++;
                     cnt0 += code == 0;
@@ -92,6 +123,7 @@ __global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, i
                     cnt3 += code == 3;
                 }
             }
+
             acc = nb ? (acc << (2 * (16 - nb))) : 0u;
             int incl = nb;
 #pragma unroll
@@ -107,6 +139,11 @@ __global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, i
             if (nb) {
                 atomicOr(&stage[wrel], acc >> (2 * sh));
                 if (sh + nb > 16) atomicOr(&stage[wrel + 1], acc << (2 * (16 - sh)));
+            }
+            if (brk && marks) {  // bits gpos .. gpos + nb - 1 of the read's break map
+                const int bs = gpos & 31;
+                atomicOr(&brk[gpos >> 5], marks << bs);
+                if (bs + nb > 32) atomicOr(&brk[(gpos >> 5) + 1], marks >> (32 - bs));
             }
             __syncwarp();
             const int nfull = ((gcount + total) >> 4) - (gcount >> 4);
@@ -128,14 +165,25 @@ __global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, i
         if (lane == 0) {
             R.len_gf[r] = gcount;
             R.comp[r] = make_int4(cnt0, cnt1, cnt2, cnt3);
-            int cw, cb, cp;
-            cutoffs(L, t, k, &cw, &cb, &cp);
+            int cw, cb, cp = 0;
+            if (R.variant == 1) cutoffs_sycl(L, t, k, &cw, &cb);
+            else cutoffs(L, t, k, &cw, &cb, &cp);
             R.cut_word[r] = cw;
             R.cut_base[r] = cb;
             R.cut_pig[r] = cp;
         }
         __syncwarp();
     }
+}
+
+// Variant 1: the window of k gap-free bases from p holds a break (bits p + 1
+// .. p + k - 1 of the read's break map), so the SYCL program has no k-mer there.
+__device__ __forceinline__ bool window_broken(const uint32_t* brk, int p, int k) {
+    const int a = p + 1, nbits = k - 1;
+    const int w = a >> 5, sh = a & 31;
+    uint64_t v = __ldg(brk + w);
+    if (sh + nbits > 32) v |= (uint64_t)__ldg(brk + w + 1) << 32;
+    return ((v >> sh) & ((1ull << nbits) - 1ull)) != 0ull;
 }
 
 template <int K>
@@ -160,7 +208,9 @@ __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
         const int nk = gf - K + 1;
         uint32_t* out = R.kmer + R.kmer_off[r];
         const uint32_t* pk = R.packed + R.pack_off[r];
+        const uint32_t* bk = R.brk ? R.brk + R.pack_off[r] : nullptr;
         for (int p = threadIdx.x; p < nk; p += blockDim.x) {
+            if (bk && window_broken(bk, p, K)) continue;
             const int w = p >> 4, o = p & 15;
             const uint64_t v = ((uint64_t)__ldg(pk + w) << 32) | __ldg(pk + w + 1);
             const uint32_t km = (uint32_t)(v >> (64 - 2 * o - 2 * K)) & (uint32_t)(NB - 1);
@@ -409,7 +459,9 @@ __global__ void __launch_bounds__(256) k_kmers_hash(DevReads R, int k) {
         __syncthreads();
         const int nk = R.len_gf[r] - k + 1;
         const uint32_t* pk = R.packed + R.pack_off[r];
+        const uint32_t* bk = R.brk ? R.brk + R.pack_off[r] : nullptr;
         for (int p = threadIdx.x; p < nk; p += blockDim.x) {
+            if (bk && window_broken(bk, p, k)) continue;
             const int w = p >> 4, o = p & 15;
             const uint64_t v = ((uint64_t)__ldg(pk + w) << 32) | __ldg(pk + w + 1);
             const uint32_t km = (uint32_t)(v >> (64 - 2 * o - 2 * k)) & mask;

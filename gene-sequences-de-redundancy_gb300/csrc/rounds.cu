@@ -42,6 +42,7 @@
 
 #include "gsdr_device.cuh"
 #include "lcs_band.cuh"
+#include "lcs_bandg.cuh"
 #include "lcs_sys.cuh"
 
 namespace gsdr {
@@ -58,7 +59,6 @@ constexpr int kFewPairs = 16384;    // queued pairs below which R grows 8x, not 
 // its pair alone, so the plain form keeps long pairs on the systolic kernels.
 constexpr int kBandMaxW = 32;
 constexpr int kPlainBandMaxW = 0;
-constexpr long long kBandMaxSerial = 16384;  // text bases x window words of one lane's pair
 
 __device__ __forceinline__ bool prefilter_pass(const int4 a, const int4 b, int cut) {
     const int s = min(a.x, b.x) + min(a.y, b.y) + min(a.z, b.z) + min(a.w, b.w);
@@ -85,23 +85,27 @@ __device__ __forceinline__ int align_class(int words) {
 // systolic length class of its pattern.  Pairs decided without alignment
 // (trivial_decision) stay in the systolic classes, which decide them.
 // A lane works through its pair alone, so only pairs whose serial work (text
-// bases x window words) stays below kBandMaxSerial go to the banded kernel; a
+// bases x window words) stays below R.band_serial go to the banded kernel; a
 // longer one would hold up its pass.
-__device__ __forceinline__ int pair_class(int T, int q, int c, int band_max_w) {
+__device__ __forceinline__ int pair_class(int T, int q, int c, int band_max_w,
+                                          long long band_serial, int group_max_w) {
     if (band_max_w > 0 && T > 0 && c > 0 && q >= c && T >= c) {
         const int bw = band_words(T, q, c);
         if (bw <= band_max_w) {
             const int w = bw <= 4 ? 4 : bw <= 8 ? 8 : bw <= 16 ? 16 : 32;
-            if ((long long)T * w <= kBandMaxSerial)
+            if ((long long)T * w <= band_serial)
                 return kSysClasses + (w == 4 ? 0 : w == 8 ? 1 : w == 16 ? 2 : 3);
         }
+        if (bw <= group_max_w) return group_class(bw);
     }
     return align_class((q + 31) >> 5);
 }
 
 __device__ __forceinline__ void queue_align(RoundState* st, Pair* pairs, int seg_cap,
                                             const DevReads& R, int rep, int q, int band_max_w) {
-    const int cls = pair_class(R.len_gf[rep], R.len_gf[q], R.cut_base[q], band_max_w);
+    const int cls =
+        pair_class(R.len_gf[rep], R.len_gf[q], R.cut_base[q], band_max_w, R.band_serial,
+                   R.group_max_w);
     const int slot = atomicAdd(&st->n_pairs[cls], 1);
     if (slot < seg_cap) pairs[(size_t)cls * seg_cap + slot] = Pair{rep, q};
     else st->pair_overflow = 1;
@@ -123,10 +127,12 @@ __device__ __forceinline__ void push_pair(RoundState* st, Pair* pairs, int seg_c
     queue_align(st, pairs, seg_cap, R, rep, q, band_max_w);
 }
 
-// Input bytes of the filter stage, counted once per launch for every
-// remaining candidate (filter_bytes): its composition, cutoffs and index
-// (28 bytes) and its (k-mer, count) list, or its k-mer bitmap in the bitmap
-// form.  Re-reads of the same bytes by other tentative groups are not counted.
+// Input bytes of the filter stage (filter_bytes), per launch for every
+// remaining candidate: its composition, cutoffs and index (28 bytes) and its
+// (k-mer, count) list, or its k-mer bitmap in the bitmap form -- in the plain
+// form only what the filter reads (no list behind a failed composition
+// bound), in the batched forms once per launch.  Re-reads of the same bytes
+// by other tentative groups are not counted.
 constexpr unsigned long long kCandFixedBytes = 16 + 8 + 4;
 __device__ __forceinline__ unsigned long long cand_bytes(const DevReads& R, int q, bool drop) {
     // (k >= 8: 4-byte k-mer ids and 2-byte counts)
@@ -174,9 +180,9 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
         const int q = remain[idx];
         if (q == rep) continue;
         n_pf++;
-        bytes += cand_bytes(R, q, DROP);
+        bytes += kCandFixedBytes;  // composition, cutoffs, index
         // kernel_preFilter (func.cu:738-754); lossless, so also used in drop mode.
-        if (!prefilter_pass(crep, R.comp[q], R.cut_base[q])) continue;
+        if (!prefilter_pass(crep, R.comp[q], R.cut_base[q] - R.strict)) continue;
         if (!DROP) {
             // kernel_filter (func.cu:803-826): S = sum over distinct k-mers of
             // min(count in representative, count in candidate), compared with
@@ -186,6 +192,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
             bool decided = false, pass = false;
             if (BITS) {
                 // D = shared k-mers (non-zero counts) bounds S: D <= S <= D + min(excesses)
+                bytes += 4ull * NBW;
                 const uint4 cb = __ldcs(reinterpret_cast<const uint4*>(R.kbits + (size_t)q * NBW) + lane % (NBW / 4));
                 int d = 0;
                 if (lane < NBW / 4) {
@@ -200,6 +207,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
             if (!decided) {
                 const int ne4 = (R.n_kmer[q] + 3) >> 2;
                 const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
+                bytes += 16ull * ne4;
                 int sum = 0;
 #pragma unroll 4
                 for (int i = lane; i < ne4; i += 32) {
@@ -314,9 +322,10 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter_g(DevReads R, RoundSt
         const int q = remain[idx];
         if (q == rep) continue;
         n_pf++;
-        bytes += cand_bytes(R, q, false);
-        if (!prefilter_pass(crep, R.comp[q], R.cut_base[q])) continue;
+        bytes += kCandFixedBytes;
+        if (!prefilter_pass(crep, R.comp[q], R.cut_base[q] - R.strict)) continue;
         n_wf++;
+        bytes += 6ull * (unsigned)R.n_kmer[q];  // k-mer ids and counts
         const uint32_t* e = R.kmer + R.kmer_off[q];
         const uint16_t* c = R.kcnt + R.kmer_off[q];
         const int ne = R.n_kmer[q];
@@ -668,6 +677,75 @@ __global__ void __launch_bounds__(kAlignThreads) k_band(DevReads R, RoundState* 
     if (cells) atomicAdd(&st->cells, cells);
 }
 
+// Banded alignment (lcs_bandg.cuh) of the pairs of group class cls: one pair
+// per group of G lanes (window of 4G words); a group whose pair is decided
+// takes the next one from the class queue at the next block of 32 text bases.
+template <int G, bool BATCH>
+__global__ void __launch_bounds__(kAlignThreads) k_bandg(DevReads R, RoundState* st, AlignArgs A,
+                                                         int cls) {
+    if (st->done) return;
+    if (BATCH && (st->pair_overflow || st->n_tent == 0)) return;
+    const int np = min(st->n_pairs[cls], A.seg_cap);
+    if (np <= 0) return;
+    const int pass = BATCH ? st->pass : 0;
+    const int lane = threadIdx.x & 31;
+    const bool leader = (lane & (G - 1)) == 0;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const Pair* list = A.pairs + (size_t)cls * A.seg_cap;
+    int* work = A.work + cls;
+    BandGroup<G> L;
+    L.init_lane(lane);
+    L.clear();
+    Pair p{-1, -1};
+    bool busy = false, more = true;
+    unsigned long long cells = 0;
+    unsigned acc = 0;
+    while (true) {
+        // idle groups take the next pairs (one atomic per warp, by the leaders)
+        unsigned need = __ballot_sync(kFull, leader && !busy);
+        while (need && more) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(work, __popc(need));
+            base = __shfl_sync(kFull, base, 0);
+            const int mine = base + __popc(need & lt_mask);  // meaningful in idle leaders
+            const int i = __shfl_sync(kFull, mine, 0, G);
+            if (!busy && i < np) {
+                const Pair pp = list[i];
+                if (pp.rep >= 0) {  // not already accepted by k_greedy
+                    p = pp;
+                    L.start(R.packed + R.pack_off[pp.cand], R.len_gf[pp.cand],
+                            R.packed + R.pack_off[pp.rep], R.len_gf[pp.rep], R.cut_base[pp.cand]);
+                    busy = true;
+                }
+            }
+            if (base + __popc(need) >= np) more = false;
+            need = __ballot_sync(kFull, leader && !busy);
+        }
+        if (!__any_sync(kFull, busy)) break;
+        uint32_t tw0 = 0, tw1 = 0;
+        if (busy) {
+            if (L.x0 < L.T) tw0 = __ldg(L.pt + (L.x0 >> 4));
+            if (L.x0 + 16 < L.T) tw1 = __ldg(L.pt + (L.x0 >> 4) + 1);
+        }
+        L.block(tw0, tw1);
+        const int d = L.finish_block(busy);
+        if (busy && d >= 0) {
+            if (leader) {
+                cells += (unsigned long long)L.T * (unsigned long long)L.q;
+                if (d) {
+                    acc++;
+                    on_accept<BATCH>(st, A, p, pass);
+                }
+            }
+            busy = false;
+            L.clear();
+        }
+    }
+    acc = (unsigned)warp_sum_i((int)acc);
+    if (!BATCH && lane == 0 && acc) atomicAdd(&st->cnt_accepted, (unsigned long long)acc);
+    if (cells) atomicAdd(&st->cells, cells);
+}
+
 __global__ void k_compact(RoundState* st, const int32_t* __restrict__ remain_in,
                           int32_t* __restrict__ remain_out, const int32_t* __restrict__ cluster) {
     if (st->done) return;
@@ -860,7 +938,8 @@ __global__ void __launch_bounds__(kTabThreads, 1) k_bfilter_tab(DevReads R, Roun
             // lane t < RG: order and composition bound of tentative t
             bool ok = false;
             if (lane < ng) {
-                ok = ttent[lane] < q && prefilter_pass(tcomp[lane], R.comp[q], R.cut_base[q]);
+                ok = ttent[lane] < q &&
+                     prefilter_pass(tcomp[lane], R.comp[q], R.cut_base[q] - R.strict);
                 n_pf += ttent[lane] < q;
             }
             const unsigned mask = __ballot_sync(kFull, ok);
@@ -961,7 +1040,8 @@ __global__ void __launch_bounds__(kFilterThreads) k_bprefilter(DevReads R, Round
             if (g == 0) bytes += cand_bytes(R, q, true);  // once per launch
             bool ok = false;
             if (lane < ng) {
-                ok = ttent[lane] < q && prefilter_pass(tcomp[lane], R.comp[q], R.cut_base[q]);
+                ok = ttent[lane] < q &&
+                     prefilter_pass(tcomp[lane], R.comp[q], R.cut_base[q] - R.strict);
                 n_pf += ttent[lane] < q;
             }
             if (ok) push_pair(st, pairs, seg_cap, R, ttent[lane], q, kBandMaxW);
@@ -1040,7 +1120,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter_bits(DevReads R, Rou
             const int q = remain[idx];
             if (g == 0) bytes += kCandFixedBytes + 16ull * NQ;  // once per launch
             const int4 cq = R.comp[q];
-            const int cbq = R.cut_base[q];
+            const int cbq = R.cut_base[q] - R.strict;  // the prefilter's cutoff
             unsigned ok_bits[RG / 32];
             bool any = false;
 #pragma unroll
@@ -1413,7 +1493,7 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
                 if (t < ntq && !(s < cw)) {
                     n_wf++;
                     const int rep = s_tent[t];
-                    if (prefilter_pass(R.comp[rep], R.comp[q], R.cut_base[q])) {
+                    if (prefilter_pass(R.comp[rep], R.comp[q], R.cut_base[q] - R.strict)) {
                         push_pair(st, pairs, seg_cap, R, rep, q, kBandMaxW);
                         n_al++;
                     }
@@ -1750,6 +1830,13 @@ void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s)
     k_align<G, W, BATCH><<<grid, kAlignThreads, smem, s>>>(R, B.st, align_args(B), cls);
 }
 
+template <int G, bool BATCH>
+void launch_bandg_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
+    static int grid = 0;
+    if (!grid) grid = grid_for(k_bandg<G, BATCH>, kAlignThreads, 0, 8);
+    k_bandg<G, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
+}
+
 template <int W, bool BATCH>
 void launch_band_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
     static int grid = 0;
@@ -1760,7 +1847,8 @@ void launch_band_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) 
 // Kernels launch_align_classes launches (after the greedy bound).
 template <bool BATCH>
 constexpr int align_launches() {
-    return kSysClasses - (BATCH ? 3 : 0) + (BATCH || kPlainBandMaxW > 0 ? kBandClasses : 0);
+    return kSysClasses - (BATCH ? 3 : 0) +
+           (BATCH || kPlainBandMaxW > 0 ? kBandClasses + kGroupClasses : 0);
 }
 
 template <bool BATCH>
@@ -1771,6 +1859,12 @@ void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bo
         launch_band_t<8, BATCH>(R, B, kSysClasses + 1, s);
         launch_band_t<16, BATCH>(R, B, kSysClasses + 2, s);
         launch_band_t<32, BATCH>(R, B, kSysClasses + 3, s);
+        constexpr int g0 = kSysClasses + kBandClasses;
+        launch_bandg_t<32, BATCH>(R, B, g0 + 4, s);  // widest windows (longest work) first
+        launch_bandg_t<16, BATCH>(R, B, g0 + 3, s);
+        launch_bandg_t<8, BATCH>(R, B, g0 + 2, s);
+        launch_bandg_t<4, BATCH>(R, B, g0 + 1, s);
+        launch_bandg_t<2, BATCH>(R, B, g0 + 0, s);
     }
     if constexpr (!BATCH) {
         launch_align_t<1, 1, BATCH>(R, B, 0, s);

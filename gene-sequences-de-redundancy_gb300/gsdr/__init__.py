@@ -40,6 +40,7 @@ class Opts(C.Structure):
         ("stage_timing", C.c_int32),
         ("verbose", C.c_int32),
         ("word_filter", C.c_int32),
+        ("variant", C.c_int32),  # 0 cuda-version semantics, 1 the SYCL program's
     ]
 
 
@@ -209,7 +210,10 @@ def _check(status):
 def default_opts(**kw) -> Opts:
     o = Opts()
     lib().gsdr_default_opts(C.byref(o))
+    names = {f[0] for f in Opts._fields_}
     for k, v in kw.items():
+        if k not in names:
+            raise TypeError(f"unknown option {k!r}")
         setattr(o, k, v)
     return o
 
@@ -336,6 +340,36 @@ def clustering(fasta: Fasta, opts: Opts | None = None, stats: bool = False, **kw
     st = Stats()
     _check(lib().gsdr_cluster(C.byref(fasta.view), C.byref(o), cl.ctypes.data, C.byref(st)))
     cl = cl[: fasta.n]
+    return (cl, st) if stats else cl
+
+
+def cluster_reads(seqs, opts: Opts | None = None, stats: bool = False, **kw):
+    """gsdr_cluster on reads the caller has already put in length order
+    (longest first, any tie order): seqs is a list of sequence byte strings.
+    Returns cluster[] in that order (and the Stats when stats=True)."""
+    o = opts if opts is not None else default_opts()
+    if kw:
+        o = Opts.from_buffer_copy(o)
+        for k, v in kw.items():
+            setattr(o, k, v)
+    lens = np.array([len(x) for x in seqs], dtype=np.int32)
+    if len(lens) > 1 and np.any(lens[1:] > lens[:-1]):
+        raise ValueError("reads must be in non-increasing length order")
+    buf = b"".join(seqs)
+    off = np.zeros(max(len(seqs), 1), dtype=np.int64)
+    if len(seqs) > 1:
+        off[1:len(seqs)] = np.cumsum(lens[:-1])
+    r = Reads()
+    keep = C.create_string_buffer(buf, max(len(buf), 1))
+    r.bytes = C.cast(keep, C.c_void_p)
+    r.n_bytes = len(buf)
+    r.offset = off.ctypes.data
+    r.length = lens.ctypes.data
+    r.n = len(seqs)
+    cl = np.empty(max(len(seqs), 1), dtype=np.int32)
+    st = Stats()
+    _check(lib().gsdr_cluster(C.byref(r), C.byref(o), cl.ctypes.data, C.byref(st)))
+    cl = cl[: len(seqs)]
     return (cl, st) if stats else cl
 
 

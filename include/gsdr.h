@@ -52,6 +52,13 @@ typedef struct {
     int32_t word_filter;  /* batched word filter form: 0 automatic, 1 per-tentative k-mer
                              tables, 2 inverted k-mer index, 3 k-mer presence bitmaps
                              (k <= 6); the result is the same in every form */
+    int32_t variant;      /* semantics: 0 = cuda-version (func.cu, the default);
+                             1 = the top-level SYCL program (func.cpp): k from t by
+                             func.cpp:36-45, w 4..8, no drop mode and no pigeon filter,
+                             k-mers over the raw read skipping windows with a non-ACGT
+                             byte (func.cpp:238-274), word cutoff in float without the
+                             offset (func.cpp:339-373), accept iff LCS > ceil(len*t)
+                             (func.cpp:671) */
 } gsdr_opts;
 
 /* Reads in length-sorted order (the order readFile leaves them in).  Read i is
@@ -75,9 +82,11 @@ typedef struct {
     int64_t pairs_accepted;
     double cells;             /* sum over aligned pairs of gap-free q x T (full-DP cells) */
     double filter_bytes;      /* input bytes of the filter stage: per launch, each remaining
-                                 candidate's (k-mer, count) list (word_index = 2: its k-mer
-                                 bitmap) and its 28 bytes of composition, cutoffs and
-                                 index, once (re-reads by other tentatives not counted) */
+                                 candidate's 28 bytes of composition, cutoffs and index and
+                                 its (k-mer, count) list (word_index = 2: its k-mer bitmap);
+                                 the plain form counts the list only where the filter
+                                 reads it (composition bound passed), the batched forms
+                                 once per launch (re-reads by other tentatives not counted) */
     double ms_h2d, ms_prep, ms_cluster, ms_d2h, ms_total;
     double ms_filter, ms_align; /* with stage_timing only */
     int32_t k, drop, pigeon, batch;
@@ -97,7 +106,8 @@ int gsdr_resolve_opts(gsdr_opts* o, const char** msg);
 
 /* checkOption (cuda-version/func.cu:10-92): argv holds letter/value pairs
  * i o t w d p; only the first character of a key counts, and a leading '-'
- * is also accepted.  Paths are copied into in_path/out_path (cap bytes each).
+ * is also accepted.  Extensions: b (batch), g (device), v (variant: 0 or 1;
+ * with v 1 the keys d and p are refused, as func.cpp:6-32 refuses them).  Paths are copied into in_path/out_path (cap bytes each).
  * Returns GSDR_OK or GSDR_EINVAL (the reference's usage exit). */
 int gsdr_check_option(int argc, char** argv, gsdr_opts* o, char* in_path, char* out_path,
                       int64_t cap);

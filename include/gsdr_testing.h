@@ -20,8 +20,9 @@ extern "C" {
  * pattern pat[k] against text txt[k]; a pattern index may appear in at most
  * one pair.  mapping: 0 = the plain form's warp grouping, 1 = the batched
  * form's, 2 = the batched form's with the banded one-pair-per-lane kernel for
- * every pair whose band fits 32 words; greedy: 1 = try the greedy-embedding
- * lower bound first.
+ * every pair whose band fits 32 words, 3 = the batched form's with the
+ * group-banded kernel (one pair per 2..32 lanes) for every pair whose band
+ * fits 128 words; greedy: 1 = try the greedy-embedding lower bound first.
  * accept[k] receives 0/1; *ms the device time of the alignment stage. */
 int gsdr_lcs_decide(const char* bytes, int64_t n_bytes, const int64_t* off, const int32_t* len,
                     int32_t n_seq, const int32_t* pat, const int32_t* txt, int32_t n_pairs,

@@ -35,6 +35,27 @@
 // rejects every candidate of a representative with no A/C/G/T base, which is
 // what the reference's drop mode does.
 //
+// Variant 1 restates the top-level SYCL program of the same repository
+// (func.cpp, a different clustering of the same inputs), selected by
+// `variant`:
+//   options          func.cpp:6-56   (checkOption: k rises with t, w 4..8,
+//                                     keys i o t w only; no drop, no pigeon)
+//   k-mers           func.cpp:238-326 (createWords/sortWords/mergeWords: every
+//                                     window of k raw bytes without a non-ACGT
+//                                     byte, u16 words, u16 multiplicities)
+//   composition      func.cpp:197-236 (raw codes 0..3: the gap-free counts)
+//   cutoffs          func.cpp:339-373 (createCutoff: float arithmetic, the
+//                                     offset forced to 1)
+//   alignment        func.cpp:572-676 (kernel_dynamic: bit-parallel LCS over
+//                                     the gap-free sequences, accept iff
+//                                     LCS > baseCutoff, strictly)
+//   loop, filters    func.cpp:447-799 (the same round structure and filters)
+// Its reader (func.cpp:70-117) gives the same reads as readFile above on a
+// file whose every line ends with '\n' (on a last line without one it does
+// not terminate), so the same reader serves both.  Parity of variant 1 is
+// pinned only by the SYCL program's own output file (the repository's
+// top-level result.fasta): no SYCL compiler is available to run it.
+//
 // Compile with -ffp-contract=off so that the cutoff arithmetic stays exact.
 
 #include <algorithm>
@@ -65,6 +86,7 @@ struct Options {
     int wordLength = 0;
     int drop = 3;
     int pigeon = 0;
+    int variant = 0;  // 0 cuda-version, 1 the SYCL program (func.cpp)
 };
 
 // checkOption (cuda-version/func.cu:10-92).  Returns 0 on success and 1 where
@@ -107,6 +129,40 @@ int check_option(int argc, char** argv, Options& o) {
     return 0;
 }
 
+// checkOption of the SYCL program (func.cpp:6-56): keys i o t w only.
+int check_option_sycl(int argc, char** argv, Options& o) {
+    if (argc % 2 != 1) return 1;
+    o = Options();
+    o.variant = 1;
+    for (int i = 1; i < argc; i += 2) {
+        try {
+            switch (argv[i][0]) {
+                case 'i': o.inputFile = argv[i + 1]; break;
+                case 'o': o.outputFile = argv[i + 1]; break;
+                case 't': o.threshold = std::stof(argv[i + 1]); break;
+                case 'w': o.wordLength = std::stoi(argv[i + 1]); break;
+                default: return 1;
+            }
+        } catch (...) {
+            return 1;
+        }
+    }
+    if (o.threshold < 0.8 || o.threshold >= 1) return 1;
+    if (o.wordLength == 0) {
+        if (o.threshold < 0.88) o.wordLength = 4;
+        else if (o.threshold < 0.94) o.wordLength = 5;
+        else if (o.threshold < 0.97) o.wordLength = 6;
+        else o.wordLength = 7;
+    } else if (o.wordLength < 4 || o.wordLength > 8) {
+        return 1;
+    }
+    o.drop = 0;
+    o.pigeon = 0;
+    return 0;
+}
+
+int g_keep_order = 0;
+
 // readFile (cuda-version/func.cu:94-117): the first line is a name whatever
 // it holds; a line starting with '>' starts the next record; every other line
 // is appended verbatim (including any '\r').  Then std::sort, longest first.
@@ -126,6 +182,12 @@ void read_file(const std::string& path, std::vector<Read>& reads) {
         read.data += line;
     }
     reads.push_back(read);
+    if (g_keep_order) {
+        // test hook: a file already in length order keeps its tie order
+        std::stable_sort(reads.begin(), reads.end(),
+                         [](const Read& a, const Read& b) { return a.data.size() > b.data.size(); });
+        return;
+    }
     std::sort(reads.begin(), reads.end(),
               [](Read& a, Read& b) { return a.data.size() > b.data.size(); });
 }
@@ -184,6 +246,48 @@ void cutoffs(int length, float threshold, int wordLength, int& word, int& base, 
     word = required;
     base = (int)std::ceil((float)((float)length * threshold));
     pigeon = (int)(std::ceil((double)(float)length * (1.0 - (double)threshold)) * 4);
+}
+
+// createCutoff of the SYCL program (func.cpp:339-373): float throughout and
+// the offset factor overwritten with 1.
+void cutoffs_sycl(int length, float threshold, int wordLength, int& word, int& base) {
+    int required = length - wordLength + 1;
+    float slack = std::ceil((float)((float)length * (float)(1.0f - threshold)));
+    int cutoff = (int)(float)(slack * (float)wordLength);
+    required -= cutoff;
+    required = std::max(required, 1);
+    required = (int)std::ceil((float)((float)required * 1.0f));
+    word = required;
+    base = (int)std::ceil((float)((float)length * threshold));
+}
+
+// createWords / sortWords / mergeWords of the SYCL program
+// (func.cpp:238-326): the window of k raw codes ending at each position,
+// skipped when it holds a code 4 (non-ACGT byte); the word puts the window's
+// last base in the low bits.  Sorted multiset with u16 multiplicities.
+void kmers_raw(const std::vector<uint8_t>& codes, int k, std::vector<uint32_t>& w,
+               std::vector<uint16_t>& c) {
+    w.clear();
+    c.clear();
+    std::vector<uint32_t> all;
+    for (int i = k - 1; i < (int)codes.size(); i++) {
+        uint32_t word = 0;
+        bool skip = false;
+        for (int j = 0; j < k; j++) {
+            uint8_t b = codes[i - j];
+            if (b == 4) skip = true;
+            word += (uint32_t)(b & 3) << (2 * j);
+        }
+        if (!skip) all.push_back(word & 0xffffu);
+    }
+    std::sort(all.begin(), all.end());
+    for (size_t i = 0; i < all.size();) {
+        size_t j = i;
+        while (j < all.size() && all[j] == all[i]) j++;
+        w.push_back(all[i]);
+        c.push_back((uint16_t)(j - i));
+        i = j;
+    }
 }
 
 // kernel_createWords / sortWords / mergeWords (cuda-version/func.cu:522-644):
@@ -293,9 +397,16 @@ void prepare(const std::vector<Read>& reads, const Options& opt, Prep& P, bool w
         }
         P.gaps[i] = (int)(s.size() - gf.size());
         pack(gf, P.packed[i]);
+        for (uint8_t b : gf) P.prefix[4 * (size_t)i + b]++;
+        if (opt.variant == 1) {
+            cutoffs_sycl(P.lengths[i], opt.threshold, opt.wordLength, P.wordCutoff[i],
+                         P.baseCutoff[i]);
+            P.pigeonCutoff[i] = 0;
+            kmers_raw(codes, opt.wordLength, P.kmer[i], P.kcnt[i]);
+            continue;
+        }
         cutoffs(P.lengths[i], opt.threshold, opt.wordLength, P.wordCutoff[i], P.baseCutoff[i],
                 P.pigeonCutoff[i]);
-        for (uint8_t b : gf) P.prefix[4 * (size_t)i + b]++;
         P.wordCounts[i] = (int)gf.size() - opt.wordLength + 1;
         if (opt.drop == 0) kmers(gf, opt.wordLength, P.kmer[i], P.kcnt[i]);
         if (want_pigeon) pigeon_index(codes, P.offsets[i], P.pig[i], P.pigIdx[i]);
@@ -402,9 +513,12 @@ inline bool word_filter(const Prep& P, const std::vector<uint16_t>& table, int q
     return !(sum < P.wordCutoff[q]);
 }
 
-// kernel_align decision (cuda-version/func.cu:885-886 and its twins).
+// kernel_align decision (cuda-version/func.cu:885-886 and its twins); for the
+// SYCL program kernel_dynamic's strict test (func.cpp:671).
+int g_variant = 0;
 inline bool align_accept(const Prep& P, int r, int q) {
     if (P.gf[r].empty()) return false;  // the reference never decides (see header)
+    if (g_variant == 1) return lcs(P.gf[r], P.gf[q]) > P.baseCutoff[q];
     return lcs(P.gf[r], P.gf[q]) >= P.baseCutoff[q];
 }
 
@@ -572,9 +686,10 @@ void orc_pigeon_index(const char* seq, int len, long long offset, uint16_t* pig2
 // sorted read i.  Returns the read count, or -1 for a usage error.
 // max_rounds < 0 runs to the end; otherwise stops after that many
 // representatives (for timing a bounded sample).
-long long orc_run(const char* in, const char* out, float t, int w, int d, int p, int lcs_mode,
-                  int threads, int max_rounds, int* order_out, int* cluster_out,
-                  orc_stats* st_out) {
+// variant 1: the SYCL program's semantics (d must be 0 or 3, p 0).
+long long orc_run_v(const char* in, const char* out, float t, int w, int d, int p, int lcs_mode,
+                    int threads, int max_rounds, int* order_out, int* cluster_out,
+                    orc_stats* st_out, int variant) {
     orc::Options o;
     o.inputFile = in;
     o.outputFile = out ? out : "";
@@ -582,23 +697,40 @@ long long orc_run(const char* in, const char* out, float t, int w, int d, int p,
     o.wordLength = w;
     o.drop = d;
     o.pigeon = p;
+    o.variant = variant;
     // Reuse check_option's derivations with the same rules.
     if (o.threshold < 0.8 || o.threshold >= 1) return -1;
-    if (o.wordLength == 0) {
-        if (o.threshold < 0.88) o.wordLength = 4;
-        else if (o.threshold < 0.94) o.wordLength = 7;
-        else if (o.threshold < 0.97) o.wordLength = 6;
-        else o.wordLength = 5;
-    } else if (o.wordLength < 4 || o.wordLength > 12) {
+    if (variant == 1) {
+        if (o.wordLength == 0) {
+            if (o.threshold < 0.88) o.wordLength = 4;
+            else if (o.threshold < 0.94) o.wordLength = 5;
+            else if (o.threshold < 0.97) o.wordLength = 6;
+            else o.wordLength = 7;
+        } else if (o.wordLength < 4 || o.wordLength > 8) {
+            return -1;
+        }
+        if ((o.drop != 0 && o.drop != 3) || o.pigeon != 0) return -1;
+        o.drop = 0;
+    } else if (variant == 0) {
+        if (o.wordLength == 0) {
+            if (o.threshold < 0.88) o.wordLength = 4;
+            else if (o.threshold < 0.94) o.wordLength = 7;
+            else if (o.threshold < 0.97) o.wordLength = 6;
+            else o.wordLength = 5;
+        } else if (o.wordLength < 4 || o.wordLength > 12) {
+            return -1;
+        }
+        if (o.drop == 3) o.drop = (o.threshold <= 0.879) ? 1 : 0;
+        else if (o.drop != 0 && o.drop != 1) return -1;
+        if (o.pigeon != 0 && o.pigeon != 1) return -1;
+    } else {
         return -1;
     }
-    if (o.drop == 3) o.drop = (o.threshold <= 0.879) ? 1 : 0;
-    else if (o.drop != 0 && o.drop != 1) return -1;
-    if (o.pigeon != 0 && o.pigeon != 1) return -1;
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
 #endif
     orc::g_lcs_mode = lcs_mode;
+    orc::g_variant = variant;
     std::vector<orc::Read> reads;
     {
         // Keep the file-order index beside each read through the sort: the
@@ -634,8 +766,11 @@ long long orc_run(const char* in, const char* out, float t, int w, int d, int p,
         };
         std::vector<Tagged> tg(file_order.size());
         for (size_t i = 0; i < file_order.size(); i++) tg[i] = {file_order[i], (int)i};
-        std::sort(tg.begin(), tg.end(),
-                  [](Tagged& a, Tagged& b) { return a.r.data.size() > b.r.data.size(); });
+        auto longer = [](const Tagged& a, const Tagged& b) {
+            return a.r.data.size() > b.r.data.size();
+        };
+        if (orc::g_keep_order) std::stable_sort(tg.begin(), tg.end(), longer);
+        else std::sort(tg.begin(), tg.end(), longer);
         for (size_t i = 0; i < tg.size(); i++) order_out[i] = tg[i].idx;
     }
     double t0 = 0;
@@ -671,6 +806,43 @@ long long orc_run(const char* in, const char* out, float t, int w, int d, int p,
     return (long long)reads.size();
 }
 
+long long orc_run(const char* in, const char* out, float t, int w, int d, int p, int lcs_mode,
+                  int threads, int max_rounds, int* order_out, int* cluster_out,
+                  orc_stats* st_out) {
+    return orc_run_v(in, out, t, w, d, p, lcs_mode, threads, max_rounds, order_out, cluster_out,
+                     st_out, 0);
+}
+
+// Test hook: 1 = read_file keeps the file's order of equal-length reads
+// (std::stable_sort) instead of the reference's std::sort order.
+void orc_set_keep_order(int keep) { orc::g_keep_order = keep; }
+
+// checkOption of the SYCL program.  Returns 0, or 1 for its usage exit.
+int orc_check_option_sycl(int argc, char** argv, float* t, int* k) {
+    orc::Options o;
+    int rc = orc::check_option_sycl(argc, argv, o);
+    if (rc) return rc;
+    *t = o.threshold;
+    *k = o.wordLength;
+    return 0;
+}
+
+void orc_cutoffs_sycl(const int* len, int n, float t, int k, int* word, int* base) {
+    for (int i = 0; i < n; i++) orc::cutoffs_sycl(len[i], t, k, word[i], base[i]);
+}
+
+// The SYCL program's k-mers of one raw sequence (sorted) with u16 counts.
+int orc_kmers_raw(const char* seq, int len, int k, uint32_t* words, uint16_t* counts) {
+    std::vector<uint8_t> codes(len);
+    for (int i = 0; i < len; i++) codes[i] = (uint8_t)orc::base_code((unsigned char)seq[i]);
+    std::vector<uint32_t> w;
+    std::vector<uint16_t> c;
+    orc::kmers_raw(codes, k, w, c);
+    std::copy(w.begin(), w.end(), words);
+    std::copy(c.begin(), c.end(), counts);
+    return (int)w.size();
+}
+
 // Pairwise decision on two raw sequences with the parameters of threshold t:
 // bit 0 prefilter pass, bit 1 word-filter pass, bit 2 LCS >= cutoff.
 // `rep` plays the representative.  Used by the known-answer test.
@@ -682,6 +854,7 @@ int orc_pair(const char* rep, int lr, const char* q, int lq, float t, int k) {
     o.threshold = t;
     o.wordLength = k;
     o.drop = 0;
+    orc::g_variant = 0;
     orc::Prep P;
     orc::prepare(reads, o, P, false);
     std::vector<uint16_t> table((size_t)1 << (2 * k), 0);

@@ -43,8 +43,38 @@ def _ties(seed=4):
 
 
 def _reference_result():
-    with gzip.open(os.path.join(HERE, "ref_cuda_result.fasta.gz"), "rb") as f:
+    return reference_result("cuda")
+
+
+def reference_result(which):
+    """The reference's own output file: "cuda" = cuda-version/result.fasta,
+    "sycl" = the SYCL program's top-level result.fasta (both at t = 0.95 on
+    the same input, which the reference does not distribute)."""
+    with gzip.open(os.path.join(HERE, f"ref_{which}_result.fasta.gz"), "rb") as f:
         return f.read()
+
+
+def records(data):
+    """(name line, sequence) pairs of a file with one sequence line per record."""
+    lines = data.split(b"\n")
+    return [(lines[i], lines[i + 1]) for i in range(0, len(lines) - 1, 2)]
+
+
+def union_of_results(first):
+    """The records of both result files, longest first; among equal lengths the
+    records of result file `first` come first, in that file's order.  Every
+    record of the other file only was absorbed, in the run that wrote `first`,
+    by a longer or earlier record of `first`, and those order ties the same
+    way here, so clustering this list with the semantics that wrote `first`
+    gives back exactly the records of `first`."""
+    mine = records(reference_result(first))
+    other = records(reference_result("sycl" if first == "cuda" else "cuda"))
+    have = set(mine)
+    rest = [r for r in other if r not in have]
+    keyed = [(len(r[1]), 0, i, r) for i, r in enumerate(mine)]
+    keyed += [(len(r[1]), 1, i, r) for i, r in enumerate(rest)]
+    keyed.sort(key=lambda x: (-x[0], x[1], x[2]))
+    return [x[3] for x in keyed], have
 
 
 # name: (input builder, cluster options as argv letters)

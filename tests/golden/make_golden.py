@@ -10,6 +10,12 @@ tests/golden/reference_outputs.json (or the path given as argument).
 
 With case names, only those cases run and their entries are merged into the
 existing output file.
+
+    python tests/golden/make_golden.py --results
+
+copies the reference's own output files (cuda-version/result.fasta and the
+SYCL program's top-level result.fasta) into tests/golden/ as
+ref_cuda_result.fasta.gz and ref_sycl_result.fasta.gz.
 """
 import hashlib
 import json
@@ -41,7 +47,25 @@ def ref_binary(max_len):
     raise RuntimeError(f"no reference build for reads of {max_len} bases")
 
 
+REFERENCE = "/root/reference"
+
+
+def copy_results():
+    import gzip
+
+    for src, dst in (("cuda-version/result.fasta", "ref_cuda_result.fasta.gz"),
+                     ("result.fasta", "ref_sycl_result.fasta.gz")):
+        with open(os.path.join(REFERENCE, src), "rb") as f:
+            data = f.read()
+        with gzip.GzipFile(os.path.join(HERE, dst), "wb", mtime=0) as g:
+            g.write(data)
+        print(dst, len(data), sha(data))
+
+
 def main():
+    if sys.argv[1:] == ["--results"]:
+        copy_results()
+        return
     import oracle_binding
 
     out_path = sys.argv[1] if len(sys.argv) > 1 else os.path.join(HERE, "reference_outputs.json")

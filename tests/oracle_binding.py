@@ -47,23 +47,42 @@ def lib():
                                        C.POINTER(C.c_int)]
         L.orc_pigeon_index.argtypes = [C.c_char_p, C.c_int, C.c_longlong, C.c_void_p,
                                        C.c_void_p]
+        L.orc_run_v.restype = C.c_longlong
+        L.orc_run_v.argtypes = L.orc_run.argtypes + [C.c_int]
+        L.orc_check_option_sycl.argtypes = [C.c_int, C.POINTER(C.c_char_p),
+                                            C.POINTER(C.c_float), C.POINTER(C.c_int)]
+        L.orc_cutoffs_sycl.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_int, C.c_void_p,
+                                       C.c_void_p]
+        L.orc_kmers_raw.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        L.orc_set_keep_order.argtypes = [C.c_int]
         _lib = L
     return _lib
 
 
-def run(path, out=None, t=0.95, w=0, d=3, p=0, lcs_mode=1, threads=0, max_rounds=-1):
-    """Runs the oracle on a FASTA file.  Returns (order, cluster, stats)."""
+def run(path, out=None, t=0.95, w=0, d=3, p=0, lcs_mode=1, threads=0, max_rounds=-1, variant=0):
+    """Runs the oracle on a FASTA file.  Returns (order, cluster, stats).
+    variant 1: the SYCL program's semantics."""
     with open(path, "rb") as f:
         n_guess = max(1, f.read().count(b"\n>") + 2)
     order = np.zeros(n_guess, dtype=np.int32)
     cluster = np.zeros(n_guess, dtype=np.int32)
     st = OrcStats()
-    n = lib().orc_run(os.fsencode(path), os.fsencode(out) if out else None, C.c_float(t), w, d,
-                      p, lcs_mode, threads, max_rounds, order.ctypes.data, cluster.ctypes.data,
-                      C.byref(st))
+    n = lib().orc_run_v(os.fsencode(path), os.fsencode(out) if out else None, C.c_float(t), w,
+                        d, p, lcs_mode, threads, max_rounds, order.ctypes.data,
+                        cluster.ctypes.data, C.byref(st), variant)
     if n < 0:
         raise ValueError("oracle rejected the options")
     return order[:n], cluster[:n], st
+
+
+def run_bytes_in_order(data: bytes, tmpdir, **kw):
+    """run_bytes on a file already in length order, keeping its order of
+    equal-length reads (a stable sort instead of the reference's std::sort)."""
+    lib().orc_set_keep_order(1)
+    try:
+        return run_bytes(data, tmpdir, **kw)
+    finally:
+        lib().orc_set_keep_order(0)
 
 
 def run_bytes(data: bytes, tmpdir, name="in.fa", **kw):
@@ -120,3 +139,27 @@ def check_option(argv):
 
 def pair(rep: bytes, q: bytes, t: float, k: int) -> int:
     return lib().orc_pair(rep, len(rep), q, len(q), C.c_float(t), k)
+
+
+def check_option_sycl(argv):
+    args = [b"cluster"] + [a.encode() for a in argv]
+    arr = (C.c_char_p * len(args))(*args)
+    t, k = C.c_float(), C.c_int()
+    if lib().orc_check_option_sycl(len(args), arr, C.byref(t), C.byref(k)):
+        return None
+    return t.value, k.value
+
+
+def cutoffs_sycl(lengths, t, k):
+    L = np.ascontiguousarray(lengths, dtype=np.int32)
+    w = np.zeros_like(L)
+    b = np.zeros_like(L)
+    lib().orc_cutoffs_sycl(L.ctypes.data, len(L), C.c_float(t), k, w.ctypes.data, b.ctypes.data)
+    return w, b
+
+
+def kmers_raw(seq: bytes, k: int):
+    w = np.zeros(max(len(seq), 1), dtype=np.uint32)
+    c = np.zeros(max(len(seq), 1), dtype=np.uint16)
+    n = lib().orc_kmers_raw(seq, len(seq), k, w.ctypes.data, c.ctypes.data)
+    return w[:n], c[:n]

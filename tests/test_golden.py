@@ -101,3 +101,40 @@ def test_cli_reproduces_reference(tmp_path):
     text = clstr.read_bytes().decode()
     assert text.count(">Cluster ") == GOLDEN["c0_3k_t90"]["records"]
     assert text.count("\n") == text.count(">Cluster ") + len(data.split(b">")) - 1
+
+
+# ---- the two reference programs' own result files --------------------------
+#
+# cuda-version/result.fasta (1,361 records) and the SYCL program's top-level
+# result.fasta (1,378 records) come from the same input (not distributed) at
+# t = 0.95 under the two programs' semantics.  Clustering the union of both
+# (longest first, ties led by the records of the file being reproduced) with
+# one program's semantics must give back exactly that program's file: 32
+# records absorbed with the cuda-version rules, 15 with the SYCL rules.
+
+@pytest.mark.parametrize("which,variant,absorbed", [("cuda", 0, 32), ("sycl", 1, 15)])
+def test_oracle_union_of_result_files(tmp_path, which, variant, absorbed):
+    recs, have = cases.union_of_results(which)
+    data = b"".join(n + b"\n" + s + b"\n" for n, s in recs)
+    _, cl, st, out = orc.run_bytes_in_order(data, tmp_path, t=0.95, variant=variant)
+    assert out == cases.reference_result(which)
+    assert st.accepted == absorbed == len(recs) - len(have)
+
+
+def test_sycl_result_file_is_a_fixed_point(tmp_path):
+    data = cases.reference_result("sycl")
+    _, cl, st, out = orc.run_bytes(data, tmp_path, t=0.95, variant=1)
+    # every record stays (std::sort may order equal lengths differently)
+    assert st.accepted == 0
+    assert sorted(cases.records(out)) == sorted(cases.records(data))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("batch", [1, 0])
+@pytest.mark.parametrize("which,variant", [("cuda", 0), ("sycl", 1)])
+def test_gpu_union_of_result_files(which, variant, batch):
+    recs, have = cases.union_of_results(which)
+    cl = gsdr.cluster_reads([s for _, s in recs], gsdr.default_opts(threshold=0.95,
+                                                                  variant=variant, batch=batch))
+    keep = [recs[i] for i in range(len(recs)) if cl[i] == i]
+    assert keep == cases.records(cases.reference_result(which))

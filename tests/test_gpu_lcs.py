@@ -2,7 +2,8 @@
 LCS(pattern, text) >= ceil(len(pattern) * t) (kernel_align,
 cuda-version/func.cu:828-999) for random, mutated and repetitive pairs in
 every length class, with both warp groupings, with the banded one-pair-per-lane
-kernel (mapping 2) and with the greedy bound."""
+kernel (mapping 2), the group-banded kernel (mapping 3) and with the greedy
+bound."""
 import numpy as np
 import pytest
 
@@ -81,7 +82,7 @@ def build_case(rng, n_pairs, qlen, tlen, kind):
     return seqs, pairs
 
 
-@pytest.mark.parametrize("mapping", [0, 1, 2])
+@pytest.mark.parametrize("mapping", [0, 1, 2, 3])
 @pytest.mark.parametrize("greedy", [0, 1])
 @pytest.mark.parametrize("qlen,tlen,kind", [
     ((20, 1000), (20, 1200), "mutated"),        # classes 0-1
@@ -118,7 +119,7 @@ def test_lcs_edge_lengths():
     seqs.append(b)
     seqs.append(b[:200] + b"NNNNNNNNNN" + b[200:400])
     pairs.append((len(seqs) - 1, len(seqs) - 2))
-    for mapping in (0, 1, 2):
+    for mapping in (0, 1, 2, 3):
         for t in (0.8, 0.9, 0.95):
             got, _ = gsdr.lcs_decide(seqs, pairs, t, mapping=mapping, greedy=1)
             np.testing.assert_array_equal(got, expected(seqs, pairs, t))
@@ -141,6 +142,30 @@ def test_band_near_threshold(t, qlen):
         pairs.append((len(seqs) - 1, len(seqs) - 2))
     want = expected(seqs, pairs, t)
     assert 0 < want.sum() < len(pairs)
-    got, _ = gsdr.lcs_decide(seqs, pairs, t, mapping=2, greedy=0)
+    for mapping in (2, 3):
+        got, _ = gsdr.lcs_decide(seqs, pairs, t, mapping=mapping, greedy=0)
+        bad = np.nonzero(got != want)[0]
+        assert len(bad) == 0, f"mapping {mapping}: {len(bad)} of {len(pairs)} differ, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("t", [0.80, 0.95])
+def test_group_band_every_class(t):
+    """Pairs whose bands need 5 to 128 window words, at both ends of each
+    group class (2, 4, 8, 16, 32 lanes x 4 words), near the threshold: the
+    group-banded kernel decides them as the full DP does."""
+    rng = np.random.default_rng(int(t * 1000))
+    seqs, pairs = [], []
+    # T - c + q - c + 62 spans window words 5 .. 128 through the lengths
+    for T in (200, 260, 400, 520, 700, 900, 1300, 1800, 2600, 3400, 5000, 6500, 9000, 12000):
+        for _ in range(6):
+            b = rand_seq(rng, T)
+            a = mutate(rng, b[: int(T * rng.uniform(0.9, 1.0))], rng.uniform(0.0, 2.0 * (1 - t)),
+                       indel=0.4)
+            seqs.append(b)
+            seqs.append(a)
+            pairs.append((len(seqs) - 1, len(seqs) - 2))
+    want = expected(seqs, pairs, t)
+    assert 0 < want.sum() < len(pairs)
+    got, _ = gsdr.lcs_decide(seqs, pairs, t, mapping=3, greedy=0)
     bad = np.nonzero(got != want)[0]
     assert len(bad) == 0, f"{len(bad)} of {len(pairs)} differ, first {bad[:5]}"

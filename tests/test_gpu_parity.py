@@ -179,3 +179,83 @@ def test_reads_above_64k_bases_are_refused():
         assert e.value.status == gsdr.EUNSUPPORTED
     finally:
         f.close()
+
+
+# ---- variant 1: the SYCL program's semantics (func.cpp) --------------------
+
+def run_both_sycl(data: bytes, tmp_path, t=0.95, w=0, batch=1):
+    order, ocl, ost, ofa = orc.run_bytes(data, tmp_path, t=t, w=w, variant=1)
+    f = gsdr.Fasta.parse(data)
+    np.testing.assert_array_equal(f.order(), order)
+    cl, st = gsdr.clustering(f, gsdr.default_opts(threshold=t, word_length=w, variant=1,
+                                                  batch=batch), stats=True)
+    out = f.format(cl)
+    f.close()
+    return cl, ocl, out, ofa, st, ost
+
+
+def n_rich_fasta(seed, n_seeds=150, copies=6):
+    """Seeds with near copies that carry non-ACGT bytes (single N, N runs,
+    IUPAC letters, lower case): k-mer windows over such bytes are where the
+    two programs' k-mer rules differ."""
+    rng = np.random.default_rng(seed)
+    codes = np.frombuffer(b"ACGT", dtype=np.uint8)
+    recs = []
+    for s in range(n_seeds):
+        L = int(rng.integers(200, 1500))
+        seed_seq = codes[rng.integers(0, 4, L)]
+        for c in range(copies):
+            seq = bytearray(seed_seq.tobytes())
+            for _ in range(int(rng.integers(0, L // 60 + 1))):
+                seq[int(rng.integers(0, L))] = int(codes[rng.integers(0, 4)])
+            for _ in range(int(rng.integers(0, 4))):
+                p = int(rng.integers(0, len(seq)))
+                run = int(rng.integers(1, 4))
+                seq[p:p + run] = bytes(rng.choice(list(b"NNNNRYSWKMn"), run))
+            if rng.random() < 0.2:
+                seq = seq.lower()
+            recs.append(b">v%d_%d\n" % (s, c) + bytes(seq) + b"\n")
+    order = rng.permutation(len(recs))
+    return b"".join(recs[i] for i in order)
+
+
+@pytest.mark.parametrize("batch", [1, 0])
+@pytest.mark.parametrize("t", [0.80, 0.85, 0.90, 0.95, 0.97])
+def test_sycl_variant_thresholds(tmp_path, t, batch):
+    data = gsdr.synth_fasta(0, n_reads=2000, seed=61)
+    cl, ocl, out, ofa, st, ost = run_both_sycl(data, tmp_path, t=t, batch=batch)
+    assert st.k == ost.k and st.drop == 0
+    assert_same(cl, ocl, out, ofa)
+    if batch == 1:
+        assert st.pairs_word == ost.prefilter_pass
+        assert st.pairs_aligned == ost.word_pass
+        assert st.pairs_accepted == ost.accepted
+
+
+@pytest.mark.parametrize("w", [4, 5, 6, 7, 8])
+def test_sycl_variant_word_lengths(tmp_path, w):
+    data = n_rich_fasta(70 + w)
+    cl, ocl, out, ofa, st, ost = run_both_sycl(data, tmp_path, t=0.93, w=w)
+    assert_same(cl, ocl, out, ofa)
+    assert st.pairs_word == ost.prefilter_pass
+    assert st.pairs_aligned == ost.word_pass
+
+
+@pytest.mark.parametrize("batch", [1, 0])
+@pytest.mark.parametrize("t", [0.90, 0.95, 0.97])
+def test_sycl_variant_n_rich(tmp_path, t, batch):
+    data = n_rich_fasta(int(t * 100))
+    cl, ocl, out, ofa, st, ost = run_both_sycl(data, tmp_path, t=t, batch=batch)
+    assert_same(cl, ocl, out, ofa)
+    if batch == 1:
+        assert st.pairs_aligned == ost.word_pass
+
+
+def test_sycl_variant_differs_from_cuda_version(tmp_path):
+    # the same input clusters differently under the two programs' rules
+    data = n_rich_fasta(5)
+    cl1, ocl1, *_ = run_both_sycl(data, tmp_path, t=0.95)
+    cl0, ocl0, *_ = run_both(data, tmp_path, t=0.95)
+    assert (ocl0 != ocl1).any()
+    np.testing.assert_array_equal(cl0, ocl0)
+    np.testing.assert_array_equal(cl1, ocl1)

@@ -161,3 +161,58 @@ def test_word_filter_option_range():
     with pytest.raises(gsdr.GsdrError):
         gsdr.resolve_opts(o)
     assert gsdr.resolve_opts(gsdr.default_opts(word_filter=2)).word_filter == 2
+
+
+# ---- variant 1: the SYCL program's option rules (func.cpp:6-56) ---------------
+
+@pytest.mark.parametrize("argv", [
+    ["t", "0.95"], ["t", "0.88"], ["t", "0.879"], ["t", "0.8"], ["t", "0.94"], ["t", "0.97"],
+    ["t", "0.93"], ["t", "0.9", "w", "8"], ["t", "0.9", "w", "9"], ["w", "3"], ["t", "1.0"],
+    ["t", "0.9", "d", "1"], ["t", "0.9", "d", "0"], ["p", "0"], ["i", "a.fa", "t", "0.91"],
+])
+def test_check_option_sycl_matches(argv):
+    ref = orc.check_option_sycl(argv)
+    try:
+        o, _, _ = gsdr.check_option(argv + ["v", "1"])
+        got = (o.threshold, o.word_length)
+        assert o.variant == 1 and o.drop == 0 and o.pigeon == 0
+    except gsdr.GsdrError as e:
+        assert e.status == gsdr.EINVAL
+        got = None
+    if ref is None:
+        assert got is None
+    else:
+        assert got is not None
+        assert np.float32(got[0]) == np.float32(ref[0]) and got[1] == ref[1]
+
+
+def test_sycl_cutoffs_are_float_formulas():
+    # func.cpp:339-373 in float32 arithmetic, offset 1; and the cuda-version
+    # formulas differ from them (double, the 1.1 - |t - 0.95| * 2 offset)
+    lens = np.arange(1, 20001, 7, dtype=np.int32)
+    for t in (0.8, 0.85, 0.9, 0.93, 0.95, 0.97, 0.99):
+        for k in (4, 5, 6, 7, 8):
+            w, b = orc.cutoffs_sycl(lens, t, k)
+            tf = np.float32(t)
+            slack = np.ceil(lens.astype(np.float32) * (np.float32(1) - tf))
+            req = lens - k + 1 - (slack * np.float32(k)).astype(np.int32)
+            np.testing.assert_array_equal(w, np.maximum(req, 1))
+            np.testing.assert_array_equal(b, np.ceil(lens.astype(np.float32) * tf).astype(np.int32))
+    w0, _, _ = orc.cutoffs(lens, 0.95, 6)
+    w1, _ = orc.cutoffs_sycl(lens, 0.95, 6)
+    assert (w0 != w1).any()
+
+
+def test_sycl_kmers_skip_windows_over_non_acgt():
+    seq = b"ACGTNACGTACGTRRACG"
+    w, c = orc.kmers_raw(seq, 4)
+    # windows of 4 raw bytes without N/R: ACGT; ACGT CGTA GTAC TACG ACGT; (none after RR but ACG is 3)
+    words = {}
+    codes = {ord("A"): 0, ord("C"): 1, ord("G"): 2, ord("T"): 3}
+    for i in range(3, len(seq)):
+        win = seq[i - 3:i + 1]
+        if all(ch in codes for ch in win):
+            v = sum(codes[win[3 - j]] << (2 * j) for j in range(4))
+            words[v] = words.get(v, 0) + 1
+    assert dict(zip(w.tolist(), c.tolist())) == words
+    assert sum(c) == 6
