@@ -226,10 +226,20 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     const bool wide = !drop && k >= kWideK;
     R.kcnt = wide ? c.take<uint16_t>((size_t)P.kmer_off[n] + 8) : nullptr;
     R.gtab = wide ? c.take<uint16_t>((size_t)1 << (2 * k)) : nullptr;
+    // (a read holds at most 4^k distinct k-mers; very long reads leave fewer
+    // CTAs counting, each with a larger table, within 256 MB of scratch)
+    int64_t distinct = std::min<int64_t>(P.max_len, (int64_t)1 << (2 * k));
     int slots = 1024;
-    while (wide && slots < 2 * P.max_len) slots <<= 1;
+    while (wide && slots < 2 * distinct) slots <<= 1;
     R.khash_slots = wide ? slots : 0;
-    R.khash = wide ? c.take<uint32_t>((size_t)kHashCtas * 3 * slots) : nullptr;
+    R.khash_ctas = wide ? (int)std::max<int64_t>(
+                              1, std::min<int64_t>(kHashCtas, (256ll << 20) / (12ll * slots)))
+                        : 0;
+    R.khash = wide ? c.take<uint32_t>((size_t)R.khash_ctas * 3 * slots) : nullptr;
+    // patterns longer than one systolic group: chunk carries of k_align_long
+    B.long_words = P.max_len > 32 * kMaxPatternWords ? (int)((P.max_len + 62) / 32 + 2) : 0;
+    B.long_carry =
+        B.long_words ? c.take<uint32_t>((size_t)num_sms() * 2 * B.long_words) : nullptr;
     const bool pig = !P.refoff16.empty();
     R.pig = pig ? c.take<uint16_t>((size_t)n * 256) : nullptr;
     R.pidx = pig ? c.take<uint16_t>((size_t)n_bytes + 8) : nullptr;
@@ -294,10 +304,20 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     Plan P;
     rc = make_plan(reads, opts, P);
     if (rc) return rc;
+    // A read with 65,536 or more k-mers can reach a word-filter sum of 65,536,
+    // which the batched filters' paired 16-bit sums do not hold: such jobs
+    // run one representative per round (32-bit sums)
+    if (batched_ && opts.drop == 0 && P.max_len - opts.word_length + 1 > 65535) {
+        batched_ = false;
+        P.r_max = 1;
+        P.idx_cap = 0;
+        P.idx_smem = false;
+        P.bits = false;
+    }
     r_max_ = P.r_max;
     stats.batch = batched_ ? r_max_ : 1;
-    if (P.max_len > 32 * kMaxPatternWords)
-        return fail(GSDR_EUNSUPPORTED, "reads above 65536 bases are not built yet");
+    if (P.max_len > kMaxReadBases)
+        return fail(GSDR_EUNSUPPORTED, "reads above 16,777,216 bases are not built yet");
     int dev_count = 0;
     if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
         return fail(GSDR_EDEVICE, "no CUDA device");

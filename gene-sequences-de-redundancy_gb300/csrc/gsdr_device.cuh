@@ -20,7 +20,9 @@
 namespace gsdr {
 
 constexpr int kMaxPatternWords = 2048;  // 8 warps x 32 lanes x 8 words: 65536 gap-free bases
-constexpr int kSysClasses = 7;          // pattern length classes of the systolic alignment kernels
+constexpr int kSysClasses = 8;          // pattern length classes of the systolic alignment kernels
+constexpr int kLongClass = kSysClasses - 1;  // patterns above kMaxPatternWords: in chunks
+constexpr int64_t kMaxReadBases = 1ll << 24;  // longest read (raw bases) a job takes
 constexpr int kBandClasses = 4;         // window classes (4, 8, 16, 32 words) of the banded kernel
 constexpr int kGroupClasses = 5;        // group-banded classes: 2, 4, 8, 16, 32 lanes x 4 words
 constexpr int kGroupMaxWords = 128;     // widest window of the group-banded kernel
@@ -86,6 +88,7 @@ struct DevReads {
     uint16_t* gtab;
     uint32_t* khash;
     int32_t khash_slots;
+    int32_t khash_ctas;  // CTAs of the hash count (each owns khash_slots slots)
     // largest serial work (text bases x window words) of a pair given to the
     // lane-per-pair banded kernel; longer pairs go to the systolic kernels
     int64_t band_serial;
@@ -160,6 +163,10 @@ struct RoundBuffers {
     int32_t* cluster;    // device, n
     int32_t* remain[2];  // device, n each
     Pair* pairs;         // device: kAlignClasses segments of seg_cap pairs
+    // reads above kMaxPatternWords * 32 bases: per block of k_align_long two
+    // buffers of long_words carry words (null when no read is that long)
+    uint32_t* long_carry;
+    int32_t long_words;
     int32_t seg_cap;
     // batched form
     int32_t* tent;       // kMaxBatch tentative read indices (ascending)

@@ -170,6 +170,12 @@ __device__ __forceinline__ int warp_sum_i(int v) {
     return v;
 }
 
+__device__ __forceinline__ unsigned long long warp_sum_ull(unsigned long long v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    return v;
+}
+
 // Returns true iff LCS(pattern, text) >= c.  pq: pattern packed words
 // (q bases); pt: text packed words (T bases).  Requires 1 <= c, q <= 1024*W.
 // STORE = keep the step's masks and sums in registers (small W) or recompute

@@ -30,6 +30,14 @@
 //           with text[0..X] and <= min(q-i, R) after, maximal at i = q-R.
 // Every wait is bounded (kSpinLimit polls) and reports an error instead of
 // hanging.
+//
+// Chunk mode (patterns above one group's 65,536 rows): the pattern is cut into
+// chunks of rows run one after another over the whole text; the top lane's
+// carry-out sequence of a chunk (one bit per text base, in 32-bit words) goes
+// to a global buffer and is the next chunk's lane-0 carry-in sequence, as
+// between the warps of a group.  The zeros of V then add up over the chunks,
+// so a chunk takes no early decision and reports its zero count at the end of
+// the text (S.result).
 #pragma once
 #include <stdint.h>
 
@@ -152,10 +160,16 @@ __host__ __device__ constexpr int sys_peq_words(int W) { return 4 * W * 32; }
 // The result lands in S.result (1 accept, 0 reject) once the group meets at
 // its barrier; S.error is set if a wait gave up.  peq: this warp's
 // sys_peq_words(W) words of shared memory for the pattern's match masks.
+// Chunk mode (chunk true): gcin (or null for the first chunk) holds the
+// carry-in words of warp 0's lane 0, gcout (or null for the last chunk)
+// receives the carry-out words of the last warp's lane 31 (a full chunk), and
+// S.result is the chunk's zero count at the end of the text.
 template <int W>
 __device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restrict__ pq, int q,
                              const uint32_t* __restrict__ pt, int T, int c, int B, int gw,
-                             int lane, int* err_flag) {
+                             int lane, int* err_flag, bool chunk = false,
+                             const uint32_t* __restrict__ gcin = nullptr,
+                             uint32_t* __restrict__ gcout = nullptr) {
     const int w0 = (gw * 32 + lane) * W;
     uint32_t V[W], snapV[W];
     peq += lane;
@@ -170,8 +184,9 @@ __device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restr
     for (int r = 0; r < 4; r++) ring[lane + 32 * r] = base_word(0, false);
     __syncwarp();
     const int M = (T + 31 + 31) >> 5;  // blocks of 32 steps: steps 0 .. T+30
-    const bool multi = B > 1;
-    const bool producer = gw < B - 1;
+    const bool multi = B > 1 || gcin != nullptr || gcout != nullptr;
+    const bool to_global = gcout != nullptr && gw == B - 1;
+    const bool producer = gw < B - 1 || to_global;
     const uint32_t not_lane0 = lane == 0 ? 0u : 0xffffffffu;
     uint32_t from = 0;   // carry from lane l-1 at the previous step
     uint32_t wprev = 0;  // top lane: carry bits of the word being completed
@@ -179,6 +194,7 @@ __device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restr
     for (int m = 0; m < M; m++) {
         if (vload(&S.stop)) return;
         uint32_t cin_word = 0;
+        if (gw == 0 && gcin) cin_word = __ldcg(gcin + m);
         if (gw > 0) {
             if (!spin_until_ge(&S.ready[gw - 1], m + 1, &S.stop)) {
                 sys_fail(S, err_flag, lane);
@@ -240,6 +256,10 @@ __device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restr
             for (int k2 = 0; k2 < nw; k2++) {
                 const int widx = m - 1 + k2;
                 if (widx < 0) continue;
+                if (to_global) {  // chunk mode: the next chunk reads it after this one
+                    if (lane == 0) __stcg(gcout + widx, k2 == 0 ? wdone : wlast);
+                    continue;
+                }
                 if (!spin_until_ge(&S.consumed[gw], widx + 1 - kSysRing, &S.stop)) {
                     sys_fail(S, err_flag, lane);
                     return;
@@ -253,7 +273,7 @@ __device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restr
         }
         // checkpoint for base 32m-1, decided by the last warp
         const int Xck = 32 * m - 1;
-        if (phase == 0 && m > 0 && Xck < T - 1) {
+        if (!chunk && phase == 0 && m > 0 && Xck < T - 1) {
             const int Rck = T - 1 - Xck;
             const int lim = q - Rck;
             const int zf_ck = warp_sum_i(zeros_below<W>(snapV, w0, q));
@@ -291,7 +311,7 @@ __device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restr
         int zt = 0;
         for (int b2 = 0; b2 < B; b2++) zt += *(volatile int*)&S.zf[b2];
         if (lane == 0) {
-            vstore(&S.result, zt >= c ? 1 : 0);
+            vstore(&S.result, chunk ? zt : (zt >= c ? 1 : 0));
             __threadfence_block();
             vstore(&S.stop, 1);
         }

@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(256) k_kmers_hash(DevReads R, int k) {
 
 __global__ void k_khash_init(DevReads R) {
     const int S = R.khash_slots;
-    const size_t total = (size_t)kHashCtas * 3 * S;
+    const size_t total = (size_t)R.khash_ctas * 3 * S;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (size_t)gridDim.x * blockDim.x) {
         const size_t part = (i / S) % 3;  // per CTA: keys, counts, slot list
@@ -516,7 +516,7 @@ int launch_kmers(const DevReads& R, int k, cudaStream_t s) {
         case 7: return kmers_hist_launch<7>(R, s);
         default:
             if (k < kWideK || k > 12 || !R.khash) return 2;
-            k_kmers_hash<<<kHashCtas, 256, 0, s>>>(R, k);
+            k_kmers_hash<<<R.khash_ctas, 256, 0, s>>>(R, k);
             return 0;
     }
 }

@@ -77,7 +77,8 @@ __device__ __forceinline__ bool prefilter_pass(const int4 a, const int4 b, int c
 // instructions per DP cell, no hand-offs between warps).
 __device__ __forceinline__ int align_class(int words) {
     return words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 256 ? 3
-                         : words <= 512 ? 4 : words <= 1024 ? 5 : 6;
+                         : words <= 512 ? 4 : words <= 1024 ? 5
+                         : words <= kMaxPatternWords ? 6 : kLongClass;
 }
 
 // Queue of a pair: a band class (kSysClasses + 0..3 for windows of 4, 8, 16,
@@ -153,6 +154,8 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
     const int rep = st->rep;
     const int n = st->n_remain;
     if (n <= 0) return;
+    // a block with no candidate skips its copy of the representative's table
+    if ((long long)blockIdx.x * (kFilterThreads / 32) >= n) return;
     if (!DROP) {
         constexpr int NB = 1 << (2 * K);
         uint32_t* t32 = reinterpret_cast<uint32_t*>(table);
@@ -744,6 +747,85 @@ __global__ void __launch_bounds__(kAlignThreads) k_bandg(DevReads R, RoundState*
     acc = (unsigned)warp_sum_i((int)acc);
     if (!BATCH && lane == 0 && acc) atomicAdd(&st->cnt_accepted, (unsigned long long)acc);
     if (cells) atomicAdd(&st->cells, cells);
+}
+
+// Pairs whose pattern has more rows than one group of 8 warps x 32 lanes x 8
+// words holds (class kLongClass): one block per pair runs the pattern in
+// chunks of 65,536 rows (lcs_sys_pair's chunk mode), the carry sequence
+// between chunks in the block's pair of global buffers; the decision is the
+// zero count summed over the chunks against the cutoff (no early exit).
+constexpr int kChunkRows = 32 * kMaxPatternWords;
+
+template <bool BATCH>
+__global__ void __launch_bounds__(kAlignThreads, 1) k_align_long(DevReads R, RoundState* st,
+                                                                 AlignArgs A, uint32_t* carry,
+                                                                 int carry_words) {
+    __shared__ SysGroup S;
+    __shared__ int s_idx;
+    extern __shared__ __align__(16) uint32_t peq_all[];  // sys_peq_words(8) per warp
+    if (st->done) return;
+    if (BATCH && (st->pair_overflow || st->n_tent == 0)) return;
+    const int np = min(st->n_pairs[kLongClass], A.seg_cap);
+    if (np <= 0 || !carry) return;
+    const int pass = BATCH ? st->pass : 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t* buf0 = carry + (size_t)blockIdx.x * 2 * carry_words;
+    uint32_t* buf1 = buf0 + carry_words;
+    unsigned long long acc = 0, cells = 0;
+    while (true) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(A.work + kLongClass, 1);
+        __syncthreads();
+        const int i = s_idx;
+        __syncthreads();
+        if (i >= np) break;
+        const Pair p = A.pairs[(size_t)kLongClass * A.seg_cap + i];
+        if (p.rep < 0) continue;  // already accepted by k_greedy
+        const int T = R.len_gf[p.rep], q = R.len_gf[p.cand], c = R.cut_base[p.cand];
+        int ok = trivial_decision(T, q, c);
+        if (ok < 0) {
+            const uint32_t* pq = R.packed + R.pack_off[p.cand];
+            const uint32_t* pt = R.packed + R.pack_off[p.rep];
+            const int nch = (q + kChunkRows - 1) / kChunkRows;
+            int ztot = 0;
+            bool err = false;
+            for (int k = 0; k < nch && !err; k++) {
+                if (threadIdx.x == 0) {
+                    for (int b = 0; b < 8; b++) {
+                        S.ready[b] = 0;
+                        S.consumed[b] = 0;
+                    }
+                    S.stop = 0;
+                    S.result = 0;
+                    S.error = 0;
+                }
+                __syncthreads();
+                const int qk = min(kChunkRows, q - k * kChunkRows);
+                const int B = (((qk + 31) >> 5) + 32 * 8 - 1) / (32 * 8);
+                const uint32_t* cin = k > 0 ? ((k & 1) ? buf0 : buf1) : nullptr;
+                uint32_t* cout = k + 1 < nch ? ((k & 1) ? buf1 : buf0) : nullptr;
+                if (warp < B)
+                    lcs_sys_pair<8>(S, peq_all + warp * sys_peq_words(8),
+                                    pq + (size_t)k * (kChunkRows / 16), qk, pt, T, c, B, warp,
+                                    lane, &st->error, true, cin, cout);
+                __syncthreads();
+                err = *(volatile int*)&S.error != 0;
+                ztot += *(volatile int*)&S.result;
+                __syncthreads();
+            }
+            ok = err ? 0 : (ztot >= c ? 1 : 0);
+        }
+        if (threadIdx.x == 0) {
+            cells += (unsigned long long)T * (unsigned long long)q;
+            if (ok) {
+                acc++;
+                on_accept<BATCH>(st, A, p, pass);
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        if (!BATCH && acc) atomicAdd(&st->cnt_accepted, acc);
+        if (cells) atomicAdd(&st->cells, cells);
+    }
 }
 
 __global__ void k_compact(RoundState* st, const int32_t* __restrict__ remain_in,
@@ -1587,7 +1669,8 @@ __global__ void k_bapply(RoundState* st, const Pair* __restrict__ acc,
     }
 }
 
-__global__ void k_badvance(RoundState* st, const int32_t* __restrict__ tent, int* align_work) {
+__global__ void k_badvance(RoundState* st, const int32_t* __restrict__ tent, int* align_work,
+                           int seg_cap, int acc_cap, int drop) {
     if (st->done) return;
     st->passes += 1;
     st->pass += 1;
@@ -1612,10 +1695,27 @@ __global__ void k_badvance(RoundState* st, const int32_t* __restrict__ tent, int
     const int surv = max(1, st->survivors);
     // a pass that queued fewer pairs than the device keeps in flight ran on
     // the latency of its longest pairs: grow R faster
-    int queued = 0;
-    for (int c = 0; c < kAlignClasses; c++) queued += st->n_pairs[c];
-    if (st->absorbed > kAbsorbHigh * surv) st->R = max(1, st->R / 2);
-    else st->R = min(st->R_max, st->R * (queued < kFewPairs ? 8 : 2));
+    int queued = 0, fullest = 0;
+    for (int c = 0; c < kAlignClasses; c++) {
+        queued += st->n_pairs[c];
+        fullest = max(fullest, st->n_pairs[c]);
+    }
+    if (st->absorbed > kAbsorbHigh * surv) {
+        st->R = max(1, st->R / 2);
+    } else {
+        // (drop mode has no filter pass to share between tentatives: R grows
+        // only while the passes are too small to fill the device, since every
+        // tentative that an earlier one absorbs wastes its alignments)
+        long long r = (long long)st->R * (queued < kFewPairs ? 8 : (drop ? 1 : 2));
+        // queue use grows with the tentatives: keep the fullest alignment
+        // queue and the accept list under 3/4 of their capacity (an overflow
+        // costs a redone pass; without the cap, drop mode, where every
+        // candidate pairs with every tentative, alternates between overflow
+        // and a small R)
+        if (nt > 0 && fullest > 0) r = min(r, (long long)nt * (3ll * seg_cap / 4) / fullest);
+        if (nt > 0 && st->n_acc > 0) r = min(r, (long long)nt * (3ll * acc_cap / 4) / st->n_acc);
+        st->R = (int)max(1ll, min((long long)st->R_max, r));
+    }
     const int n = st->n_next;
     st->n_next = 0;
     st->next_min = 0x7fffffff;
@@ -1844,10 +1944,23 @@ void launch_band_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) 
     k_band<W, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
 }
 
+template <bool BATCH>
+void launch_align_long_t(const DevReads& R, RoundBuffers& B, cudaStream_t s) {
+    constexpr int smem = (kAlignThreads / 32) * sys_peq_words(8) * 4;
+    static bool set = false;
+    if (!set) {
+        cudaFuncSetAttribute(k_align_long<BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+        set = true;
+    }
+    k_align_long<BATCH><<<num_sms(), kAlignThreads, smem, s>>>(R, B.st, align_args(B),
+                                                               B.long_carry, B.long_words);
+}
+
 // Kernels launch_align_classes launches (after the greedy bound).
 template <bool BATCH>
-constexpr int align_launches() {
-    return kSysClasses - (BATCH ? 3 : 0) +
+int align_launches(const RoundBuffers& B) {
+    return kSysClasses - 1 - (BATCH ? 3 : 0) + (B.long_carry ? 1 : 0) +
            (BATCH || kPlainBandMaxW > 0 ? kBandClasses + kGroupClasses : 0);
 }
 
@@ -1891,6 +2004,7 @@ void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bo
         launch_align_t<8, 4, BATCH>(R, B, 5, s);
         launch_align_t<8, 8, BATCH>(R, B, 6, s);
     }
+    if (B.long_carry) launch_align_long_t<BATCH>(R, B, s);
 }
 
 }  // namespace
@@ -1922,7 +2036,7 @@ void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity
     k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, align_work_of(B.st));
     if (ev4) cudaEventRecord(ev4[3], s);
     if (count)
-        *count += 4 + align_launches<false>() + (R.pig_q && !drop ? 1 : 0) +
+        *count += 4 + align_launches<false>(B) + (R.pig_q && !drop ? 1 : 0) +
                   (!drop && R.k >= kWideK ? 2 : 0);
 }
 
@@ -1934,7 +2048,8 @@ void launch_align_stage(const DevReads& R, RoundBuffers& B, bool batched_mapping
 
 int align_class_host(int words) {
     return words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 256 ? 3
-                         : words <= 512 ? 4 : words <= 1024 ? 5 : 6;
+                         : words <= 512 ? 4 : words <= 1024 ? 5
+                         : words <= kMaxPatternWords ? 6 : kLongClass;
 }
 
 void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,
@@ -1954,10 +2069,10 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     k_bclaim<<<g, 256, 0, s>>>(B.st, B.acc, B.tidx, B.survive, B.best);
     k_bapply<<<g, 256, 0, s>>>(B.st, B.acc, B.tidx, B.best, B.cluster);
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
-    k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st));
+    k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st), B.seg_cap, B.acc_cap, drop);
     if (ev4) cudaEventRecord(ev4[3], s);
     if (count)
-        *count += 8 + align_launches<true>() + (!drop && (B.idx_off || B.amb) ? 1 : 0) +
+        *count += 8 + align_launches<true>(B) + (!drop && (B.idx_off || B.amb) ? 1 : 0) +
                   (R.pig_q && !drop ? 1 : 0);
 }
 

@@ -170,8 +170,42 @@ def test_reads_above_32k_bases(tmp_path, batch):
     assert st.pairs_accepted == ost.accepted
 
 
-def test_reads_above_64k_bases_are_refused():
-    data = b">a\n" + b"ACGT" * 16500 + b"\n>b\nACGT\n"
+@pytest.mark.parametrize("batch", [1, 0])
+def test_reads_above_65536_bases(tmp_path, batch):
+    """Patterns above one systolic group's 65,536 rows run in chunks
+    (k_align_long): near copies of a 140 kbp read and of a 70 kbp one, with
+    the 140 kbp read's halves and some unrelated long reads."""
+    rng = np.random.default_rng(17)
+    codes = np.frombuffer(b"ACGT", dtype=np.uint8)
+    recs = []
+    for s, L in enumerate((140000, 70000, 66000)):
+        base = bytearray(codes[rng.integers(0, 4, L)].tobytes())
+        for c in range(3):
+            seq = bytearray(base)
+            for _ in range(int(rng.integers(0, L // 40))):
+                seq[int(rng.integers(0, len(seq)))] = int(codes[rng.integers(0, 4)])
+            for _ in range(int(rng.integers(0, 30))):
+                p = int(rng.integers(0, len(seq)))
+                if rng.random() < 0.5:
+                    del seq[p]
+                else:
+                    seq.insert(p, int(codes[rng.integers(0, 4)]))
+            recs.append(b">L%d_%d\n" % (s, c) + bytes(seq) + b"\n")
+        if s == 0:
+            recs.append(b">half\n" + bytes(base[:69000]) + b"\n")
+    data = b"".join(recs)
+    for t in (0.90, 0.97):
+        cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=t, batch=batch)
+        assert_same(cl, ocl, out, ofa)
+        assert st.pairs_accepted == ost.accepted
+        assert st.batch == 1  # reads with 65,536+ k-mers: one representative per round
+    # drop mode keeps the batched form (no word filter)
+    cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.85, batch=batch)
+    assert_same(cl, ocl, out, ofa)
+
+
+def test_reads_above_the_length_limit_are_refused():
+    data = b">a\n" + b"ACGT" * (1 << 22) + b"A\n>b\nACGT\n"
     f = gsdr.Fasta.parse(data)
     try:
         with pytest.raises(gsdr.GsdrError) as e:
