@@ -339,11 +339,16 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
               R_, B_);
     stats.word_index = P.idx_cap > 0 ? 1 : (P.bits ? 2 : 0);
     R_.threshold = opts.threshold;
-    R_.band_serial = kBandMaxSerial;
-    if (const char* bs = std::getenv("GSDR_BAND_SERIAL")) R_.band_serial = std::atoll(bs);
-    R_.group_max_w = kGroupMaxWords;
-    if (const char* gw = std::getenv("GSDR_GROUP_MAXW"))
-        R_.group_max_w = std::min(std::max(std::atoi(gw), 0), kGroupMaxWords);
+    // band tiles of the banded alignment kernels (gsdr_opts; 0 = automatic,
+    // where the environment may still override the defaults)
+    R_.band_serial = opts.band_serial > 0 ? opts.band_serial : opts.band_serial < 0 ? 0 : kBandMaxSerial;
+    if (opts.band_serial == 0)
+        if (const char* bs = std::getenv("GSDR_BAND_SERIAL")) R_.band_serial = std::atoll(bs);
+    R_.group_max_w = opts.group_words > 0 ? std::min(opts.group_words, kGroupMaxWords)
+                                          : opts.group_words < 0 ? 0 : kGroupMaxWords;
+    if (opts.group_words == 0)
+        if (const char* gw = std::getenv("GSDR_GROUP_MAXW"))
+            R_.group_max_w = std::min(std::max(std::atoi(gw), 0), kGroupMaxWords);
     refoff16_.swap(P.refoff16);
     pack_off_.swap(P.pack_off);
     kmer_off_.swap(P.kmer_off);
@@ -414,13 +419,33 @@ int Job::loop_graph() {
 int Job::loop_timed() {
     cudaEvent_t e4[4] = {};
     for (auto& e : e4) JCUDA(cudaEventCreate(&e));
+    // One graph per remain-buffer parity holding one step's kernels with event
+    // records between its stages (external event nodes): the step's launches
+    // reach the device together, so the events time the device work alone and
+    // not the host's launch calls.
+    cudaGraph_t g[2] = {};
+    cudaGraphExec_t gx[2] = {};
+    long long per_step = 0;
+    int rc = GSDR_OK;
+    for (int p = 0; p < 2 && rc == GSDR_OK; p++) {
+        long long per = 0;
+        cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            launch_step(p, &per, e4);
+            e = cudaStreamEndCapture(stream, &g[p]);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&gx[p], g[p], 0);
+        if (e != cudaSuccess) rc = cuda_fail(e, "timed step capture");
+        per_step = per;
+    }
     int parity = 0;
     double fms = 0, ams = 0;
     long long launches = 0;
-    int rc = GSDR_OK;
-    while (true) {
-        launch_step(parity, &launches, e4);
-        cudaError_t e = cudaGetLastError();
+    unsigned long long fbytes_prev = 0;
+    stats.filter_max_bytes = stats.filter_max_ms = 0;
+    while (rc == GSDR_OK) {
+        cudaError_t e = cudaGraphLaunch(gx[parity], stream);
+        launches += per_step;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(h_done_, &B_.st->done, sizeof(int32_t), cudaMemcpyDeviceToHost,
                                 stream);
@@ -434,6 +459,17 @@ int Job::loop_timed() {
         cudaEventElapsedTime(&b, e4[1], e4[2]);
         fms += a;
         ams += b;
+        // input bytes of this step's filter launch: the counter's growth
+        unsigned long long fbytes = 0;
+        if (cudaMemcpy(&fbytes, &B_.st->filter_bytes, sizeof(fbytes), cudaMemcpyDeviceToHost) ==
+            cudaSuccess) {
+            const double step_bytes = (double)(fbytes - fbytes_prev);
+            if (step_bytes > stats.filter_max_bytes) {
+                stats.filter_max_bytes = step_bytes;
+                stats.filter_max_ms = a;
+            }
+            fbytes_prev = fbytes;
+        }
         if (trace_) {
             // per-step trace on stderr: the state after the step
             RoundState h;
@@ -458,6 +494,10 @@ int Job::loop_timed() {
     stats.ms_filter = fms;
     stats.ms_align = ams;
     stats.kernel_launches += launches;
+    for (int p = 0; p < 2; p++) {
+        if (gx[p]) cudaGraphExecDestroy(gx[p]);
+        if (g[p]) cudaGraphDestroy(g[p]);
+    }
     for (auto& e : e4) cudaEventDestroy(e);
     return rc;
 }
@@ -468,6 +508,8 @@ int Job::run(int pass_limit) {
     const int k = opts.word_length;
     const bool drop = opts.drop == 1;
     stats.kernel_launches = 0;
+    stats.ms_filter = stats.ms_align = 0;
+    stats.filter_max_bytes = stats.filter_max_ms = 0;
     JCUDA(cudaSetDevice(opts.device));
     JCUDA(cudaEventRecord(ev_[1], stream));
     // baseToNumber + compressData + createCutoff + createPrefix (func.cu:139-403)

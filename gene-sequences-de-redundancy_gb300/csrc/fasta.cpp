@@ -340,6 +340,10 @@ int gsdr_resolve_opts(gsdr_opts* o, const char** msg) {
         m = "word filter form must be 0..3";
     } else if (o->variant != 0 && o->variant != 1) {
         m = "variant must be 0 (cuda-version) or 1 (SYCL program)";
+    } else if (o->band_serial < -1) {
+        m = "band_serial must be -1, 0 or positive";
+    } else if (o->group_words < -1 || o->group_words > 128) {
+        m = "group_words must be -1..128";
     } else if (o->variant == 1 && o->word_length != 0 &&
                (o->word_length < 4 || o->word_length > 8)) {
         m = "word length out of range (4<=word length<=8)";  // func.cpp:47-51

@@ -142,16 +142,23 @@ __device__ __forceinline__ unsigned long long cand_bytes(const DevReads& R, int 
 
 // ---------------------------------------------------------------- plain form
 
+// tent: null in the plain form.  In the batched form (table filter) this
+// kernel takes the passes with a single tentative: that tentative is the
+// smallest unclustered read, so every other remaining read is its candidate
+// and the pass is a plain round; k_bfilter_tab takes the passes with more.
 template <int K, bool DROP>
-__global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundState* st,
+__global__ void __launch_bounds__(kFilterThreads, 6) k_filter(DevReads R, RoundState* st,
                                                            const int32_t* __restrict__ remain,
-                                                           Pair* pairs, int seg_cap) {
+                                                           Pair* pairs, int seg_cap,
+                                                           const int32_t* __restrict__ tent) {
     extern __shared__ __align__(16) uint16_t table[];
     constexpr bool BITS = !DROP && K <= kMaxBitsK;
     constexpr int NBW = BITS ? (1 << (2 * K)) / 32 : 4;
     __shared__ __align__(16) uint32_t rbits[NBW];
     if (st->done) return;
-    const int rep = st->rep;
+    if (tent && st->n_tent != 1) return;
+    const int rep = tent ? tent[0] : st->rep;
+    const int band_w = tent ? kBandMaxW : kPlainBandMaxW;
     const int n = st->n_remain;
     if (n <= 0) return;
     // a block with no candidate skips its copy of the representative's table
@@ -226,7 +233,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_filter(DevReads R, RoundStat
             if (!pass) continue;
         }
         n_al++;
-        if (lane == 0) push_pair(st, pairs, seg_cap, R, rep, q, kPlainBandMaxW);
+        if (lane == 0) push_pair(st, pairs, seg_cap, R, rep, q, band_w);
     }
     if (lane == 0) {
         if (n_pf) atomicAdd(&st->cnt_prefilter, (unsigned long long)n_pf);
@@ -974,7 +981,8 @@ __global__ void __launch_bounds__(kTabThreads, 1) k_bfilter_tab(DevReads R, Roun
     extern __shared__ __align__(16) uint16_t tab[];  // [NB][RG]
     __shared__ int4 tcomp[RG];
     __shared__ int ttent[RG];
-    if (st->done || st->n_tent == 0) return;
+    // a pass with a single tentative is k_filter's (launched before this one)
+    if (st->done || st->n_tent <= 1) return;
     const int nt = st->n_tent;
     const int n = st->n_remain;
     const int ngroups = (nt + RG - 1) / RG;
@@ -1768,8 +1776,11 @@ int grid_for(KernelT kernel, int threads, int smem, int cap_per_sm) {
     return num_sms() * per_sm;
 }
 
+// tent: null for a plain round; the batched form's tentatives otherwise (the
+// kernel then runs only in a pass with a single tentative).
 template <int K, bool DROP>
-void launch_filter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, cudaStream_t s) {
+void launch_filter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, cudaStream_t s,
+                     const int32_t* tent = nullptr) {
     const int smem = DROP ? 0 : (1 << (2 * K)) * 2;
     static int grid = 0;
     if (!grid) {
@@ -1778,12 +1789,17 @@ void launch_filter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, 
                                  smem);
         grid = grid_for(k_filter<K, DROP>, kFilterThreads, smem, 8);
     }
-    k_filter<K, DROP><<<grid, kFilterThreads, smem, s>>>(R, B.st, remain, B.pairs, B.seg_cap);
+    k_filter<K, DROP><<<grid, kFilterThreads, smem, s>>>(R, B.st, remain, B.pairs, B.seg_cap,
+                                                         tent);
 }
 
 template <int K>
 void launch_bfilter_tab_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
                           cudaStream_t s) {
+    // passes with one tentative (the first passes of adaptive R) stream the
+    // candidates once against one table: the plain kernel does that at HBM
+    // speed, the grouped-table kernel skips them
+    launch_filter_t<K, false>(R, B, remain, s, B.tent);
     constexpr int smem = TabGroup<K>::smem;
     static int grid = 0;
     if (!grid) {
@@ -2026,15 +2042,15 @@ void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity
                         long long* count, cudaEvent_t* ev4) {
     const int32_t* rin = B.remain[parity];
     int32_t* rout = B.remain[parity ^ 1];
-    if (ev4) cudaEventRecord(ev4[0], s);
+    if (ev4) cudaEventRecordWithFlags(ev4[0], s, cudaEventRecordExternal);
     launch_filter_any<false>(R, B, rin, drop, s);
     if (R.pig_q && !drop) k_pigeon<false><<<num_sms() * 8, 256, 0, s>>>(R, B.st, B.pairs, B.seg_cap);
-    if (ev4) cudaEventRecord(ev4[1], s);
+    if (ev4) cudaEventRecordWithFlags(ev4[1], s, cudaEventRecordExternal);
     launch_align_classes<false>(R, B, s);
-    if (ev4) cudaEventRecord(ev4[2], s);
+    if (ev4) cudaEventRecordWithFlags(ev4[2], s, cudaEventRecordExternal);
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_advance<<<1, 1, 0, s>>>(B.st, B.cluster, align_work_of(B.st));
-    if (ev4) cudaEventRecord(ev4[3], s);
+    if (ev4) cudaEventRecordWithFlags(ev4[3], s, cudaEventRecordExternal);
     if (count)
         *count += 4 + align_launches<false>(B) + (R.pig_q && !drop ? 1 : 0) +
                   (!drop && R.k >= kWideK ? 2 : 0);
@@ -2058,21 +2074,21 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     int32_t* rout = B.remain[parity ^ 1];
     k_bselect<<<1, 1024, 0, s>>>(B.st, B.cluster, R.n, B.tent, B.tidx, B.tt, B.ttrow, B.survive,
                                  align_work_of(B.st));
-    if (ev4) cudaEventRecord(ev4[0], s);
+    if (ev4) cudaEventRecordWithFlags(ev4[0], s, cudaEventRecordExternal);
     launch_filter_any<true>(R, B, rin, drop, s);
     if (R.pig_q && !drop) k_pigeon<true><<<num_sms() * 8, 256, 0, s>>>(R, B.st, B.pairs, B.seg_cap);
-    if (ev4) cudaEventRecord(ev4[1], s);
+    if (ev4) cudaEventRecordWithFlags(ev4[1], s, cudaEventRecordExternal);
     launch_align_classes<true>(R, B, s);
-    if (ev4) cudaEventRecord(ev4[2], s);
+    if (ev4) cudaEventRecordWithFlags(ev4[2], s, cudaEventRecordExternal);
     k_bsurvive<<<1, 32, 0, s>>>(B.st, B.tent, B.tt, B.ttrow, B.survive, B.cluster);
     const int g = num_sms() * 2;
     k_bclaim<<<g, 256, 0, s>>>(B.st, B.acc, B.tidx, B.survive, B.best);
     k_bapply<<<g, 256, 0, s>>>(B.st, B.acc, B.tidx, B.best, B.cluster);
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
     k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st), B.seg_cap, B.acc_cap, drop);
-    if (ev4) cudaEventRecord(ev4[3], s);
+    if (ev4) cudaEventRecordWithFlags(ev4[3], s, cudaEventRecordExternal);
     if (count)
-        *count += 8 + align_launches<true>(B) + (!drop && (B.idx_off || B.amb) ? 1 : 0) +
+        *count += 8 + align_launches<true>(B) + (!drop ? 1 : 0) +
                   (R.pig_q && !drop ? 1 : 0);
 }
 

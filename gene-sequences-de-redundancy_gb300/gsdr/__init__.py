@@ -41,6 +41,8 @@ class Opts(C.Structure):
         ("verbose", C.c_int32),
         ("word_filter", C.c_int32),
         ("variant", C.c_int32),  # 0 cuda-version semantics, 1 the SYCL program's
+        ("band_serial", C.c_int32),  # lane-banded kernel's limit; 0 automatic, -1 none
+        ("group_words", C.c_int32),  # group-banded kernel's widest window; 0 automatic, -1 none
     ]
 
 
@@ -77,6 +79,8 @@ class Stats(C.Structure):
         ("batch", C.c_int32),
         ("kernel_launches", C.c_int64),
         ("word_index", C.c_int32),
+        ("filter_max_bytes", C.c_double),
+        ("filter_max_ms", C.c_double),
     ]
 
     def as_dict(self):

@@ -59,6 +59,13 @@ typedef struct {
                              byte (func.cpp:238-274), word cutoff in float without the
                              offset (func.cpp:339-373), accept iff LCS > ceil(len*t)
                              (func.cpp:671) */
+    int32_t band_serial;  /* band tile of the lane-per-pair banded alignment kernel: the
+                             largest serial work (text bases x window words) of a pair it
+                             takes; 0 = automatic (16,384), -1 = none (those pairs go to
+                             the other alignment kernels); the result is the same */
+    int32_t group_words;  /* band tile of the group-banded alignment kernel: the widest
+                             band window (32-bit words, 1..128) it takes; 0 = automatic
+                             (128), -1 = none; the result is the same */
 } gsdr_opts;
 
 /* Reads in length-sorted order (the order readFile leaves them in).  Read i is
@@ -95,6 +102,9 @@ typedef struct {
                                  tables, 1 per-pass inverted k-mer index (reads holding
                                  few of the 4^k k-mers), 2 k-mer presence bitmaps with
                                  an exact sum for the pairs their bound leaves open */
+    double filter_max_bytes;  /* with stage_timing only: input bytes of the filter launch
+                                 that read the most, and its time (filter_max_ms) */
+    double filter_max_ms;
 } gsdr_stats;
 
 /* Fill `o` with the reference defaults (t 0.95, derived k/drop, pigeon 0). */

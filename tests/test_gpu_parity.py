@@ -105,6 +105,22 @@ def test_c2_recipe_slice(tmp_path):
     assert_same(cl, ocl, out, ofa)
 
 
+@pytest.mark.parametrize("cfg,n,t", [(2, 6000, 0.90), (0, 3000, 0.85), (1, 3000, 0.95)])
+@pytest.mark.parametrize("group_words,band_serial", [(-1, -1), (8, 1 << 30), (32, 4096),
+                                                     (128, 65536)])
+def test_band_tiles_same_clusters(tmp_path, cfg, n, t, group_words, band_serial):
+    # the band tiles only move pairs between alignment kernels
+    data = gsdr.synth_fasta(cfg, n_reads=n, seed=51 + cfg)
+    _, ocl, _, _ = orc.run_bytes(data, tmp_path, t=t)
+    f = gsdr.Fasta.parse(data)
+    try:
+        cl = gsdr.clustering(f, gsdr.default_opts(threshold=t, group_words=group_words,
+                                                  band_serial=band_serial))
+    finally:
+        f.close()
+    np.testing.assert_array_equal(cl, ocl)
+
+
 def test_c3_recipe_slice_drop(tmp_path):
     data = gsdr.synth_fasta(3, n_reads=120, seed=41)
     cl, ocl, out, ofa, st, ost = run_both(data, tmp_path, t=0.80)

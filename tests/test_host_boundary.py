@@ -163,6 +163,21 @@ def test_word_filter_option_range():
     assert gsdr.resolve_opts(gsdr.default_opts(word_filter=2)).word_filter == 2
 
 
+@pytest.mark.parametrize("kw", [{"group_words": 129}, {"group_words": -2},
+                                {"band_serial": -2}])
+def test_band_tile_option_range(kw):
+    with pytest.raises(gsdr.GsdrError) as e:
+        gsdr.resolve_opts(gsdr.default_opts(**kw))
+    assert e.value.status == gsdr.EINVAL
+
+
+def test_band_tile_options_default_to_automatic():
+    o = gsdr.resolve_opts(gsdr.default_opts(group_words=-1, band_serial=4096))
+    assert (o.group_words, o.band_serial) == (-1, 4096)
+    d = gsdr.default_opts()
+    assert (d.group_words, d.band_serial) == (0, 0)
+
+
 # ---- variant 1: the SYCL program's option rules (func.cpp:6-56) ---------------
 
 @pytest.mark.parametrize("argv", [
