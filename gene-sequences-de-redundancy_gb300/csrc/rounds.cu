@@ -966,7 +966,13 @@ template <int K>
 struct TabGroup {
     static constexpr int RG = K <= 5 ? 32 : K == 6 ? 16 : 4;
     static constexpr int NB = 1 << (2 * K);
-    static constexpr int smem = NB * RG * 2;  // 64 KB (k 5), 128 KB (k 6, 7)
+    // u16 per k-mer row: the group's RG counts, padded by 16 bytes where a
+    // row is read with 16-byte loads.  A warp reads random rows; with a
+    // 32-byte (64-byte) stride the first 16 bytes of a row fall in only 4 (2)
+    // of the 8 16-byte bank groups of a 128-byte line, with 48 (80) bytes in
+    // all 8, which cuts the bank conflicts of a quarter-warp's loads.
+    static constexpr int ROW = RG >= 8 ? RG + 8 : RG;
+    static constexpr int smem = NB * ROW * 2;  // 80 KB (k 5), 192 KB (k 6), 128 KB (k 7)
 };
 constexpr int kTabThreads = 1024;
 
@@ -976,9 +982,10 @@ __global__ void __launch_bounds__(kTabThreads, 1) k_bfilter_tab(DevReads R, Roun
                                                                 const int32_t* __restrict__ tent,
                                                                 Pair* pairs, int seg_cap) {
     constexpr int RG = TabGroup<K>::RG;
+    constexpr int ROW = TabGroup<K>::ROW;
     constexpr int W = RG / 2;  // packed sums per lane
     constexpr int WARPS = kTabThreads / 32;
-    extern __shared__ __align__(16) uint16_t tab[];  // [NB][RG]
+    extern __shared__ __align__(16) uint16_t tab[];  // [NB][ROW], RG counts used per row
     __shared__ int4 tcomp[RG];
     __shared__ int ttent[RG];
     // a pass with a single tentative is k_filter's (launched before this one)
@@ -1014,7 +1021,7 @@ __global__ void __launch_bounds__(kTabThreads, 1) k_bfilter_tab(DevReads R, Roun
                 for (int i = lane; i < ne; i += 32) {
                     const uint32_t v = __ldg(e + i);
                     const uint32_t c = v & 0xffffu;
-                    if (c) tab[(v >> 16) * RG + t] = (uint16_t)c;
+                    if (c) tab[(v >> 16) * ROW + t] = (uint16_t)c;
                 }
             }
             __syncthreads();
@@ -1047,7 +1054,7 @@ __global__ void __launch_bounds__(kTabThreads, 1) k_bfilter_tab(DevReads R, Roun
                 for (int e = 0; e < 4; e++) {
                     const uint32_t c = ev[e] & 0xffffu;
                     const uint32_t cc = c | (c << 16);
-                    const uint32_t* row = reinterpret_cast<const uint32_t*>(tab + (ev[e] >> 16) * RG);
+                    const uint32_t* row = reinterpret_cast<const uint32_t*>(tab + (ev[e] >> 16) * ROW);
                     if constexpr (RG >= 8) {
 #pragma unroll
                         for (int w = 0; w < W; w += 4) {
@@ -1618,10 +1625,24 @@ __global__ void k_bsurvive(RoundState* st, const int32_t* __restrict__ tent,
     for (int w = 0; w < kTTWords; w++) {
         uint32_t rw = __shfl_sync(kFull, rows, w);
         while (rw) {
-            const int h = w * 32 + __ffs(rw) - 1;
-            rw &= rw - 1;
-            const uint32_t cw = __shfl_sync(kFull, claimed, h >> 5);
-            if (!((cw >> (h & 31)) & 1u)) claimed |= tt[h * kTTWords + lane];
+            // the next eight rows with bits: their words are loaded together
+            // (they do not depend on the claims), then applied in order
+            constexpr int P = 8;
+            int hs[P];
+            uint32_t v[P];
+#pragma unroll
+            for (int j = 0; j < P; j++) {
+                hs[j] = rw ? w * 32 + __ffs(rw) - 1 : -1;
+                rw &= rw - 1u;
+            }
+#pragma unroll
+            for (int j = 0; j < P; j++) v[j] = hs[j] >= 0 ? tt[hs[j] * kTTWords + lane] : 0u;
+#pragma unroll
+            for (int j = 0; j < P; j++) {
+                if (hs[j] < 0) break;  // warp-uniform
+                const uint32_t cw = __shfl_sync(kFull, claimed, hs[j] >> 5);
+                if (!((cw >> (hs[j] & 31)) & 1u)) claimed |= v[j];
+            }
         }
     }
     uint32_t valid;
