@@ -118,11 +118,11 @@ __device__ __forceinline__ void hyyro_step(uint32_t (&V)[W], const uint32_t (&H)
 // The same step with the match masks read from a table in shared memory
 // instead of formed from the bit planes (that moves two logic operations per
 // word off the integer pipe, which bounds these kernels): pm[32 * i] is the
-// match mask of word i for this step's base (one lane's row of the table);
-// inv is all ones for "no base" (U = 0).
+// match mask of word i for this step's base (one lane's row of the table;
+// the all-zero row for "no base" gives U = 0).
 template <int W>
 __device__ __forceinline__ void peq_step(uint32_t (&V)[W], const uint32_t* __restrict__ pm,
-                                         uint32_t inv, uint32_t& cy) {
+                                         uint32_t& cy) {
     constexpr int C = W >= 4 ? 4 : W;
 #pragma unroll
     for (int i = 0; i < W; i += C) {
@@ -130,7 +130,7 @@ __device__ __forceinline__ void peq_step(uint32_t (&V)[W], const uint32_t* __res
 #pragma unroll
         for (int j = 0; j < C; j++) {
             m[j] = pm[32 * (i + j)];
-            u[j] = V[i + j] & m[j] & ~inv;
+            u[j] = V[i + j] & m[j];
         }
         if constexpr (C == 4)
             add4_carry(s[0], s[1], s[2], s[3], V[i], V[i + 1], V[i + 2], V[i + 3], u[0], u[1],
@@ -146,9 +146,10 @@ __device__ __forceinline__ void peq_step(uint32_t (&V)[W], const uint32_t* __res
 
 // Match-mask table of one lane's W pattern words: peq[(b * W + i) * 32] =
 // positions of word i holding base b (b = 0..3; lane-interleaved, so a warp's
-// lanes read consecutive words).  Positions past the pattern match base 0,
-// as the zero bit planes do in hyyro_step; their carries only move upward
-// and their bits are never counted.
+// lanes read consecutive words), and row b = 4 all zero (a step that must
+// leave V unchanged).  Positions past the pattern match base 0, as the zero
+// bit planes do in hyyro_step; their carries only move upward and their bits
+// are never counted.
 template <int W>
 __device__ __forceinline__ void peq_fill(uint32_t* peq, const uint32_t* __restrict__ pq, int q,
                                          int w0) {
@@ -161,6 +162,7 @@ __device__ __forceinline__ void peq_fill(uint32_t* peq, const uint32_t* __restri
         peq[(1 * W + i) * 32] = ~h & l;
         peq[(2 * W + i) * 32] = h & ~l;
         peq[(3 * W + i) * 32] = h & l;
+        peq[(4 * W + i) * 32] = 0u;
     }
 }
 

@@ -12,15 +12,16 @@
 // top lane's carry-out sequence (one bit per text base) is the next warp's
 // lane-0 carry-in sequence, handed over in 32-bit words through a ring in
 // shared memory.  Text bases come from a per-warp 64-entry ring (written twice
-// so that a lane-skewed window is contiguous), one 32-bit word per base: its
-// 2-bit code and a "no base" flag in bit 31.  A step reads its match masks
-// from the lane's row of a per-warp table in shared memory indexed by the code
-// (peq_step), which keeps the integer pipe for the recurrence itself.
+// so that a lane-skewed window is contiguous), one 32-bit word per base: the
+// offset of the base's rows in a per-warp table of match masks in shared
+// memory (peq_step reads the lane's column there), which keeps the integer
+// pipe for the recurrence itself and costs a step no decoding of the base.
 //
 // Bases outside the text ("no base": pipeline fill before base 0, drain after
-// base T-1) must leave V unchanged.  The flag only clears U: with U = 0 and a
-// zero carry-in, V + U + 0 = V and V' = V | (V & ~M) = V for any M; the carry
-// out is then zero too, so by induction every carry-in of such a step is zero.
+// base T-1) must leave V unchanged.  Their ring entry points at a fifth, all-
+// zero row of the table: with M = 0, U = V & M = 0, and with a zero carry-in
+// V + U + 0 = V and V' = V | (V & ~M) = V; the carry out is then zero too, so
+// by induction every carry-in of such a step is zero.
 //
 // Decisions, taken every kSysCk blocks of 32 bases by the group's last warp
 // from the zero counts every warp publishes:
@@ -50,19 +51,23 @@ constexpr int kSysZRing = 16;   // checkpoints kept per warp
 constexpr int kSysCk = 4;       // blocks of 32 bases between checkpoints
 constexpr int kSpinLimit = 1 << 22;
 
-struct SysGroup {
-    uint32_t carries[8][kSysRing];
-    int zc[8][kSysZRing];    // zeros of the warp's words at a checkpoint
-    int zp[8][kSysZRing];    // zeros below q - R at that checkpoint
-    int zf[8];               // zeros at the end of the text
-    int ready[8];            // carry words published by warp b
-    int consumed[8];         // carry words of warp b read by warp b+1
-    uint32_t ring[8][128];   // text bases, sign-coded bytes
+// Shared state of a group of up to NW warps deciding one pair.
+template <int NW>
+struct SysGroupT {
+    static constexpr int kWarps = NW;
+    uint32_t carries[NW][kSysRing];
+    int zc[NW][kSysZRing];    // zeros of the warp's words at a checkpoint
+    int zp[NW][kSysZRing];    // zeros below q - R at that checkpoint
+    int zf[NW];               // zeros at the end of the text
+    int ready[NW];            // carry words published by warp b
+    int consumed[NW];         // carry words of warp b read by warp b+1
+    uint32_t ring[NW][128];   // text bases: their row offsets in the match-mask table
     int stop;
     int result;
     int idx;
     int error;
 };
+using SysGroup = SysGroupT<8>;
 
 __device__ __forceinline__ int vload(const int* p) { return *(volatile const int*)p; }
 __device__ __forceinline__ void vstore(int* p, int v) { *(volatile int*)p = v; }
@@ -93,12 +98,15 @@ __device__ __forceinline__ int zeros_below(const uint32_t (&V)[W], int w0, int l
     return z;
 }
 
-// Ring entry of a text base: the 2-bit code, bit 31 set for "no base".
-__device__ __forceinline__ uint32_t base_word(uint32_t code, bool valid) {
-    return valid ? (code & 3u) : 0x80000000u;
+// Ring entry of a text base: the word offset of its rows in the match-mask
+// table (rows of 32 * W words per base code; row 4 is all zero, for "no base").
+template <int W>
+__device__ __forceinline__ uint32_t base_row(uint32_t code, bool valid) {
+    return (valid ? (code & 3u) : 4u) * (32u * W);
 }
 
-__device__ __forceinline__ void sys_fail(SysGroup& S, int* err_flag, int lane) {
+template <class Group>
+__device__ __forceinline__ void sys_fail(Group& S, int* err_flag, int lane) {
     if (lane == 0) {
         atomicExch(err_flag, 1);
         vstore(&S.error, 1);
@@ -121,9 +129,7 @@ __device__ __forceinline__ void sys_steps8(const uint32_t* __restrict__ rb,
     for (int j = 0; j < 8; j++) {
         uint32_t cin = from;
         if (MULTI) cin = not_lane0 ? from : ((cin8 >> j) & 1u);
-        const uint32_t b = rb[j];
-        const uint32_t inv = (uint32_t)((int32_t)b >> 31);
-        peq_step<W>(V, peq + (b & 3u) * (32u * W), inv, cin);
+        peq_step<W>(V, peq + rb[j], cin);
         if (MULTI) out8 |= cin << j;
         // lane 0 receives its own carry-out from the shuffle: a single warp
         // clears it (its lane-0 carry-in is zero); a group member ignores it
@@ -153,8 +159,9 @@ __device__ __forceinline__ void sys_block(const uint32_t* __restrict__ rb,
     }
 }
 
-// Shared memory of one warp's match-mask table (sys_peq_words(W) words).
-__host__ __device__ constexpr int sys_peq_words(int W) { return 4 * W * 32; }
+// Shared memory of one warp's match-mask table (sys_peq_words(W) words): rows
+// for the four base codes and the all-zero "no base" row.
+__host__ __device__ constexpr int sys_peq_words(int W) { return 5 * W * 32; }
 
 // The decision of one pair on B warps of a group (gw = this warp's index).
 // The result lands in S.result (1 accept, 0 reject) once the group meets at
@@ -164,8 +171,8 @@ __host__ __device__ constexpr int sys_peq_words(int W) { return 4 * W * 32; }
 // carry-in words of warp 0's lane 0, gcout (or null for the last chunk)
 // receives the carry-out words of the last warp's lane 31 (a full chunk), and
 // S.result is the chunk's zero count at the end of the text.
-template <int W>
-__device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restrict__ pq, int q,
+template <int W, class Group>
+__device__ void lcs_sys_pair(Group& S, uint32_t* peq, const uint32_t* __restrict__ pq, int q,
                              const uint32_t* __restrict__ pt, int T, int c, int B, int gw,
                              int lane, int* err_flag, bool chunk = false,
                              const uint32_t* __restrict__ gcin = nullptr,
@@ -181,7 +188,7 @@ __device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restr
     }
     uint32_t* ring = S.ring[gw];
 #pragma unroll
-    for (int r = 0; r < 4; r++) ring[lane + 32 * r] = base_word(0, false);
+    for (int r = 0; r < 4; r++) ring[lane + 32 * r] = base_row<W>(0, false);
     __syncwarp();
     const int M = (T + 31 + 31) >> 5;  // blocks of 32 steps: steps 0 .. T+30
     const bool multi = B > 1 || gcin != nullptr || gcout != nullptr;
@@ -211,7 +218,7 @@ __device__ void lcs_sys_pair(SysGroup& S, uint32_t* peq, const uint32_t* __restr
             const int x = 32 * m + lane;
             uint32_t code = 0;
             if (x < T) code = (__ldg(pt + (x >> 4)) >> (30 - 2 * (x & 15))) & 3u;
-            const uint32_t bw = base_word(code, x < T);
+            const uint32_t bw = base_row<W>(code, x < T);
             ring[x & 63] = bw;
             ring[(x & 63) + 64] = bw;
         }

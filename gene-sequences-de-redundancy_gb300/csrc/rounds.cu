@@ -485,7 +485,7 @@ template <int G, int W, bool BATCH>
 __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundState* st, AlignArgs A,
                                                          int cls) {
     constexpr int NG = (kAlignThreads / 32) / G;
-    __shared__ SysGroup groups[NG];
+    __shared__ SysGroupT<G> groups[NG];
     extern __shared__ __align__(16) uint32_t peq_all[];  // sys_peq_words(W) per warp
     if (st->done) return;
     if (BATCH && (st->pair_overflow || st->n_tent == 0)) return;
@@ -494,11 +494,11 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
     const int pass = BATCH ? st->pass : 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = warp / G, gw = warp % G;
-    SysGroup& S = groups[g];
+    SysGroupT<G>& S = groups[g];
     const int bar_id = 1 + g, bar_n = G * 32;
     const Pair* list = A.pairs + (size_t)cls * A.seg_cap;
     if (gw == 0 && lane == 0) {
-        for (int b = 0; b < 8; b++) {
+        for (int b = 0; b < G; b++) {
             S.ready[b] = 0;
             S.consumed[b] = 0;
         }
@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
                 acc++;
                 on_accept<BATCH>(st, A, p, pass);
             }
-            for (int b = 0; b < 8; b++) {
+            for (int b = 0; b < G; b++) {
                 S.ready[b] = 0;
                 S.consumed[b] = 0;
             }
@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
 // ones fill in behind them (one kernel tail per pass instead of four).
 __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, RoundState* st,
                                                                    AlignArgs A, int* work) {
-    __shared__ SysGroup groups[kAlignThreads / 32];
+    __shared__ SysGroupT<1> groups[kAlignThreads / 32];  // one single-warp group per warp
     extern __shared__ __align__(16) uint32_t peq_all[];  // sys_peq_words(8) per warp
     if (st->done) return;
     if (st->pair_overflow || st->n_tent == 0) return;
@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, R
     if (total <= 0) return;
     const int pass = st->pass;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    SysGroup& S = groups[warp];
+    SysGroupT<1>& S = groups[warp];
     unsigned long long cells = 0;
     while (true) {
         int i = 0;
