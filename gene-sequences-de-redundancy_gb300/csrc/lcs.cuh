@@ -85,6 +85,52 @@ __device__ __forceinline__ void add4_carry(uint32_t& s0, uint32_t& s1, uint32_t&
         : "r"(v0), "r"(v1), "r"(v2), "r"(v3), "r"(u0), "r"(u1), "r"(u2), "r"(u3));
 }
 
+// The same chains with an enable of the carry in: the chain starts from
+// cy + en, which carries out iff cy = 1 and en = ~0, so en = 0 ignores cy (a
+// lane whose carry-in must be zero passes 0 instead of clearing cy first).
+__device__ __forceinline__ void add1_carry_en(uint32_t& s0, uint32_t v0, uint32_t u0, uint32_t& cy,
+                                           uint32_t en) {
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "add.cc.u32 t, %1, %4;\n\t"
+        "addc.cc.u32 %0, %2, %3;\n\t"
+        "addc.u32 %1, 0, 0;\n\t"
+        "}"
+        : "=r"(s0), "+r"(cy)
+        : "r"(v0), "r"(u0), "r"(en));
+}
+
+__device__ __forceinline__ void add2_carry_en(uint32_t& s0, uint32_t& s1, uint32_t v0, uint32_t v1,
+                                           uint32_t u0, uint32_t u1, uint32_t& cy,
+                                           uint32_t en) {
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "add.cc.u32 t, %2, %7;\n\t"
+        "addc.cc.u32 %0, %3, %5;\n\t"
+        "addc.cc.u32 %1, %4, %6;\n\t"
+        "addc.u32 %2, 0, 0;\n\t"
+        "}"
+        : "=r"(s0), "=r"(s1), "+r"(cy)
+        : "r"(v0), "r"(v1), "r"(u0), "r"(u1), "r"(en));
+}
+
+__device__ __forceinline__ void add4_carry_en(uint32_t& s0, uint32_t& s1, uint32_t& s2, uint32_t& s3,
+                                           uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3,
+                                           uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3,
+                                           uint32_t& cy, uint32_t en) {
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "add.cc.u32 t, %4, %13;\n\t"
+        "addc.cc.u32 %0, %5, %9;\n\t"
+        "addc.cc.u32 %1, %6, %10;\n\t"
+        "addc.cc.u32 %2, %7, %11;\n\t"
+        "addc.cc.u32 %3, %8, %12;\n\t"
+        "addc.u32 %4, 0, 0;\n\t"
+        "}"
+        : "=r"(s0), "=r"(s1), "=r"(s2), "=r"(s3), "+r"(cy)
+        : "r"(v0), "r"(v1), "r"(v2), "r"(v3), "r"(u0), "r"(u1), "r"(u2), "r"(u3), "r"(en));
+}
+
 // One text base applied to W pattern words (Hyyro's LCS recurrence):
 //   M = match mask of the base (from the pattern's high / low bit planes H, Lo
 //   and the base's bits as full masks ch, cl), U = V & M & keep,
@@ -119,10 +165,11 @@ __device__ __forceinline__ void hyyro_step(uint32_t (&V)[W], const uint32_t (&H)
 // instead of formed from the bit planes (that moves two logic operations per
 // word off the integer pipe, which bounds these kernels): pm[32 * i] is the
 // match mask of word i for this step's base (one lane's row of the table;
-// the all-zero row for "no base" gives U = 0).
+// the all-zero row for "no base" gives U = 0).  en = 0 ignores the carry in
+// (add*_carry).
 template <int W>
 __device__ __forceinline__ void peq_step(uint32_t (&V)[W], const uint32_t* __restrict__ pm,
-                                         uint32_t& cy) {
+                                         uint32_t& cy, uint32_t en = 0xffffffffu) {
     constexpr int C = W >= 4 ? 4 : W;
 #pragma unroll
     for (int i = 0; i < W; i += C) {
@@ -132,13 +179,15 @@ __device__ __forceinline__ void peq_step(uint32_t (&V)[W], const uint32_t* __res
             m[j] = pm[32 * (i + j)];
             u[j] = V[i + j] & m[j];
         }
+        // the carry between chunks of the lane's words is always taken
+        const uint32_t e = i == 0 ? en : 0xffffffffu;
         if constexpr (C == 4)
-            add4_carry(s[0], s[1], s[2], s[3], V[i], V[i + 1], V[i + 2], V[i + 3], u[0], u[1],
-                       u[2], u[3], cy);
+            add4_carry_en(s[0], s[1], s[2], s[3], V[i], V[i + 1], V[i + 2], V[i + 3], u[0],
+                          u[1], u[2], u[3], cy, e);
         else if constexpr (C == 2)
-            add2_carry(s[0], s[1], V[i], V[i + 1], u[0], u[1], cy);
+            add2_carry_en(s[0], s[1], V[i], V[i + 1], u[0], u[1], cy, e);
         else
-            add1_carry(s[0], V[i], u[0], cy);
+            add1_carry_en(s[0], V[i], u[0], cy, e);
 #pragma unroll
         for (int j = 0; j < C; j++) V[i + j] = s[j] | (V[i + j] & ~m[j]);
     }

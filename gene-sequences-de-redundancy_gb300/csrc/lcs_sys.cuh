@@ -129,12 +129,14 @@ __device__ __forceinline__ void sys_steps8(const uint32_t* __restrict__ rb,
     for (int j = 0; j < 8; j++) {
         uint32_t cin = from;
         if (MULTI) cin = not_lane0 ? from : ((cin8 >> j) & 1u);
-        peq_step<W>(V, peq + rb[j], cin);
+        // lane 0 of a single warp has a zero carry-in: its carry enable is
+        // not_lane0 = 0 (its `from` is its own carry-out, from the shuffle)
+        peq_step<W>(V, peq + rb[j], cin, MULTI ? 0xffffffffu : not_lane0);
         if (MULTI) out8 |= cin << j;
         // lane 0 receives its own carry-out from the shuffle: a single warp
-        // clears it (its lane-0 carry-in is zero); a group member ignores it
+        // ignores it through the carry enable above, a group member through
+        // the select of the previous warp's carry bits
         from = __shfl_up_sync(0xffffffffu, cin, 1);
-        if (!MULTI) from &= not_lane0;
         if (SNAP && jbase + j == tj) {
 #pragma unroll
             for (int i = 0; i < W; i++) snapV[i] = V[i];
