@@ -21,15 +21,19 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "gsdr.h"
 #include "gsdr_device.cuh"
 #include "gsdr_host.h"
 #include "job.h"
+#include "stdsort.h"
 
 struct gsdr_result {
     std::vector<char> out;          // representative records, saveFile's bytes
@@ -375,6 +379,25 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
         ~StreamGuard() { cudaStreamDestroy(s); }
     } sg{s};
     const double t0 = now_ms();
+    // GSDR_TRACE=1: host time at each phase's end (the stream synchronized
+    // there, so the phases do not overlap), on stderr
+    const char* tr = std::getenv("GSDR_TRACE");
+    const bool trace = tr && tr[0] == '1';
+    std::vector<std::pair<const char*, double>> marks;
+    auto mark = [&](const char* what) {
+        if (!trace) return;
+        cudaStreamSynchronize(s);
+        marks.emplace_back(what, now_ms() - t0);
+    };
+    struct TracePrint {
+        const std::vector<std::pair<const char*, double>>& m;
+        ~TracePrint() {
+            if (m.empty()) return;
+            std::string line = "gsdr trace: cluster_fasta";
+            for (auto& x : m) line += " " + std::string(x.first) + " " + std::to_string(x.second);
+            std::fprintf(stderr, "%s ms\n", line.c_str());
+        }
+    } tp{marks};
 
     // the file on the device, with room for multi-line records' data after it
     // (at most the file's size) and 16 bytes of slack for word loads
@@ -383,6 +406,7 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     DCUDA(cudaMemsetAsync(file.as<uint8_t>() + n, 0, 64, s));
     DCUDA(cudaMemcpyAsync(file.p, fasta, (size_t)n, cudaMemcpyHostToDevice, s));
     uint8_t* b = file.as<uint8_t>();
+    mark("h2d");
 
     const int64_t n_chunks = (n + kChunk - 1) / kChunk;
     const int64_t per = (int64_t)kScanThreads * kScanItems;
@@ -442,6 +466,7 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
             data_len.as<int64_t>(), pieces.as<int32_t>());
     }
     DCUDA(cudaGetLastError());
+    mark("parse");
     std::vector<int64_t> h_dlen(n_rec), h_doff(n_rec);
     std::vector<int32_t> h_pieces(n_rec);
     DCUDA(cudaMemcpyAsync(h_dlen.data(), data_len.p, sizeof(int64_t) * n_rec,
@@ -470,15 +495,18 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
             pieces.as<int32_t>(), data_off.as<int64_t>());
         DCUDA(cudaGetLastError());
     }
-    // readFile's std::sort (func.cu:111-113) on the record indices
+    // readFile's std::sort (func.cu:111-113) on the record indices (the same
+    // permutation, its independent parts on several threads: stdsort.h)
     const int32_t nr = (int32_t)n_rec;
     res->order.resize(nr);
     std::iota(res->order.begin(), res->order.end(), 0);
+    mark("records");
     std::vector<int32_t> dl(nr);
     for (int32_t r = 0; r < nr; r++) dl[r] = (int32_t)h_dlen[r];
     const int32_t* dlp = dl.data();
-    std::sort(res->order.begin(), res->order.end(),
-              [dlp](const int32_t& a, const int32_t& c) { return dlp[a] > dlp[c]; });
+    std_sort_threaded(res->order.begin(), res->order.end(),
+                      [dlp](const int32_t& a, const int32_t& c) { return dlp[a] > dlp[c]; },
+                      sort_threads());
     std::vector<int64_t> s_off(nr);
     res->length.resize(nr);
     for (int32_t i = 0; i < nr; i++) {
@@ -486,6 +514,7 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
         res->length[i] = dl[res->order[i]];
     }
     const double t_parse = now_ms();
+    mark("sort");
 
     // the clustering on the device-resident reads
     // (bytes: the device copy; the job reads only sizes from the view on the host)
@@ -494,8 +523,11 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     res->cluster.assign(nr > 0 ? nr : 1, 0);
     Job job;
     rc = job.init(&view, &o, s);
+    mark("job_init");
     if (!rc) rc = job.upload(&view, b);
+    mark("upload");
     if (!rc) rc = job.run();
+    mark("run");
     if (rc) return rc;
     // the output records, formatted on the device
     DevBuf d_order, sz;
@@ -529,7 +561,9 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     } else {
         return fail(GSDR_EUNSUPPORTED, "device formatting of files above 4 GiB");
     }
+    mark("output");
     rc = job.download(res->cluster.data());
+    mark("download");
     if (rc) return rc;
     res->cluster.resize(nr);
     job.stats.ms_total = now_ms() - t0;

@@ -15,6 +15,7 @@
 
 #include "gsdr.h"
 #include "gsdr_host.h"
+#include "stdsort.h"
 
 struct gsdr_fasta {
     std::vector<char> buf;          // file bytes, then concatenated multi-line records
@@ -102,10 +103,12 @@ int parse_into(gsdr_fasta* f) {
     std::iota(f->order.begin(), f->order.end(), 0);
     // Same call as func.cu:111-113 (std::sort, length descending).  The
     // permutation depends only on the comparison outcomes, so sorting indices
-    // reproduces the reference's order of equal-length reads.
+    // reproduces the reference's order of equal-length reads; large inputs
+    // run the same sort's independent parts on several threads (stdsort.h).
     const int32_t* dl = f->data_len.data();
-    std::sort(f->order.begin(), f->order.end(),
-              [dl](const int32_t& a, const int32_t& c) { return dl[a] > dl[c]; });
+    gsdr::std_sort_threaded(f->order.begin(), f->order.end(),
+                            [dl](const int32_t& a, const int32_t& c) { return dl[a] > dl[c]; },
+                            gsdr::sort_threads());
     f->s_off.resize(count);
     f->s_len.resize(count);
     for (int32_t i = 0; i < count; i++) {

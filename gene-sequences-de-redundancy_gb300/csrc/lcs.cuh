@@ -114,6 +114,21 @@ __device__ __forceinline__ void add2_carry_en(uint32_t& s0, uint32_t& s1, uint32
         : "r"(v0), "r"(v1), "r"(u0), "r"(u1), "r"(en));
 }
 
+__device__ __forceinline__ void add3_carry_en(uint32_t& s0, uint32_t& s1, uint32_t& s2,
+                                              uint32_t v0, uint32_t v1, uint32_t v2, uint32_t u0,
+                                              uint32_t u1, uint32_t u2, uint32_t& cy, uint32_t en) {
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "add.cc.u32 t, %3, %10;\n\t"
+        "addc.cc.u32 %0, %4, %7;\n\t"
+        "addc.cc.u32 %1, %5, %8;\n\t"
+        "addc.cc.u32 %2, %6, %9;\n\t"
+        "addc.u32 %3, 0, 0;\n\t"
+        "}"
+        : "=r"(s0), "=r"(s1), "=r"(s2), "+r"(cy)
+        : "r"(v0), "r"(v1), "r"(v2), "r"(u0), "r"(u1), "r"(u2), "r"(en));
+}
+
 __device__ __forceinline__ void add4_carry_en(uint32_t& s0, uint32_t& s1, uint32_t& s2, uint32_t& s3,
                                            uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3,
                                            uint32_t u0, uint32_t u1, uint32_t u2, uint32_t u3,
@@ -170,26 +185,36 @@ __device__ __forceinline__ void hyyro_step(uint32_t (&V)[W], const uint32_t (&H)
 template <int W>
 __device__ __forceinline__ void peq_step(uint32_t (&V)[W], const uint32_t* __restrict__ pm,
                                          uint32_t& cy, uint32_t en = 0xffffffffu) {
-    constexpr int C = W >= 4 ? 4 : W;
+    // the lane's words in add-with-carry chains of four, then one of W % 4;
+    // the carry between chains is always taken
+    constexpr int NFULL = W / 4, TAIL = W % 4;
 #pragma unroll
-    for (int i = 0; i < W; i += C) {
-        uint32_t m[C], u[C], s[C];
+    for (int k = 0; k < NFULL; k++) {
+        const int i = 4 * k;
+        uint32_t m[4], s[4];
 #pragma unroll
-        for (int j = 0; j < C; j++) {
-            m[j] = pm[32 * (i + j)];
-            u[j] = V[i + j] & m[j];
-        }
-        // the carry between chunks of the lane's words is always taken
-        const uint32_t e = i == 0 ? en : 0xffffffffu;
-        if constexpr (C == 4)
-            add4_carry_en(s[0], s[1], s[2], s[3], V[i], V[i + 1], V[i + 2], V[i + 3], u[0],
-                          u[1], u[2], u[3], cy, e);
-        else if constexpr (C == 2)
-            add2_carry_en(s[0], s[1], V[i], V[i + 1], u[0], u[1], cy, e);
+        for (int j = 0; j < 4; j++) m[j] = pm[32 * (i + j)];
+        add4_carry_en(s[0], s[1], s[2], s[3], V[i], V[i + 1], V[i + 2], V[i + 3], V[i] & m[0],
+                      V[i + 1] & m[1], V[i + 2] & m[2], V[i + 3] & m[3], cy,
+                      k == 0 ? en : 0xffffffffu);
+#pragma unroll
+        for (int j = 0; j < 4; j++) V[i + j] = s[j] | (V[i + j] & ~m[j]);
+    }
+    if constexpr (TAIL > 0) {
+        constexpr int i = 4 * NFULL;
+        const uint32_t e = NFULL == 0 ? en : 0xffffffffu;
+        uint32_t m[TAIL], s[TAIL];
+#pragma unroll
+        for (int j = 0; j < TAIL; j++) m[j] = pm[32 * (i + j)];
+        if constexpr (TAIL == 3)
+            add3_carry_en(s[0], s[1], s[2], V[i], V[i + 1], V[i + 2], V[i] & m[0],
+                          V[i + 1] & m[1], V[i + 2] & m[2], cy, e);
+        else if constexpr (TAIL == 2)
+            add2_carry_en(s[0], s[1], V[i], V[i + 1], V[i] & m[0], V[i + 1] & m[1], cy, e);
         else
-            add1_carry_en(s[0], V[i], u[0], cy, e);
+            add1_carry_en(s[0], V[i], V[i] & m[0], cy, e);
 #pragma unroll
-        for (int j = 0; j < C; j++) V[i + j] = s[j] | (V[i + j] & ~m[j]);
+        for (int j = 0; j < TAIL; j++) V[i + j] = s[j] | (V[i + j] & ~m[j]);
     }
 }
 

@@ -596,10 +596,18 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, R
             const uint32_t* pq = R.packed + R.pack_off[p.cand];
             const uint32_t* pt = R.packed + R.pack_off[p.rep];
             uint32_t* peq = peq_all + warp * sys_peq_words(8);
-            switch (cls) {
-                case 0: lcs_sys_pair<1>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 1: lcs_sys_pair<2>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 2: lcs_sys_pair<4>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+            // words per lane: the fewest that hold the pattern (1024 bases
+            // each over the warp), not the class's power of two -- a step
+            // costs about three integer ops per word plus three
+            const int wl = (q + 1023) >> 10;  // 1..8 in these classes (q <= 8192)
+            switch (wl) {
+                case 1: lcs_sys_pair<1>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 2: lcs_sys_pair<2>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 3: lcs_sys_pair<3>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 4: lcs_sys_pair<4>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 5: lcs_sys_pair<5>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 6: lcs_sys_pair<6>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 7: lcs_sys_pair<7>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
                 default: lcs_sys_pair<8>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
             }
             __syncwarp();

@@ -144,7 +144,7 @@ def lib():
         L.gsdr_fasta_format.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                         P(C.c_int64)]
         L.gsdr_fasta_free.argtypes = [C.c_void_p]
-        L.gsdr_cluster_fasta.argtypes = [C.c_char_p, C.c_int64, P(Opts), P(C.c_void_p),
+        L.gsdr_cluster_fasta.argtypes = [C.c_void_p, C.c_int64, P(Opts), P(C.c_void_p),
                                          P(Stats)]
         L.gsdr_result_output.argtypes = [C.c_void_p, P(C.c_void_p), P(C.c_int64)]
         L.gsdr_result_count.argtypes = [C.c_void_p]
@@ -414,16 +414,30 @@ class Job:
             pass
 
 
-def cluster_fasta(data: bytes, opts: Opts | None = None, stats: bool = False, **kw):
+def _host_bytes(data):
+    """(pointer, size) of FASTA bytes given as bytes or as a uint8 numpy array
+    (for example a view of pinned host memory, whose copy to the device is
+    faster than a copy from pageable memory)."""
+    if isinstance(data, bytes):
+        return C.cast(C.c_char_p(data), C.c_void_p), len(data)
+    a = np.asarray(data)
+    if a.dtype != np.uint8 or a.ndim != 1 or not a.flags.c_contiguous:
+        raise TypeError("FASTA bytes: bytes or a contiguous 1-D uint8 array")
+    return C.c_void_p(a.ctypes.data), a.nbytes
+
+
+def cluster_fasta(data, opts: Opts | None = None, stats: bool = False, **kw):
     """readFile + clustering + saveFile on the device (gsdr_cluster_fasta):
-    FASTA bytes in; returns (output FASTA bytes, cluster[] in sorted order,
-    the sort permutation), and the Stats when stats=True."""
+    FASTA bytes in (bytes, or a uint8 array such as a view of pinned host
+    memory); returns (output FASTA bytes, cluster[] in sorted order, the sort
+    permutation), and the Stats when stats=True."""
     o = opts if opts is not None else default_opts()
     for k, v in kw.items():
         setattr(o, k, v)
     st = Stats()
     h = C.c_void_p()
-    _check(lib().gsdr_cluster_fasta(data, len(data), C.byref(o), C.byref(h), C.byref(st)))
+    ptr, size = _host_bytes(data)
+    _check(lib().gsdr_cluster_fasta(ptr, size, C.byref(o), C.byref(h), C.byref(st)))
     try:
         ptr, n = C.c_void_p(), C.c_int64()
         _check(lib().gsdr_result_output(h, C.byref(ptr), C.byref(n)))

@@ -85,3 +85,19 @@ def test_device_parse_c2_slice_ties():
     assert out == hout
     np.testing.assert_array_equal(order, horder)
     assert st.rounds > 0
+
+
+def test_device_parse_large_ties_match_std_sort(tmp_path):
+    # 100k reads of 150 bp (>= 65,536 records: the host sort runs threaded):
+    # the order is std::sort's tie-breaking alone, checked against the oracle
+    import oracle_binding as orc
+
+    data = gsdr.synth_fasta(2, n_reads=100000, seed=73)
+    path = tmp_path / "c2_100k.fa"
+    path.write_bytes(data)
+    oorder, _, _ = orc.run(str(path), None, t=0.99, d=1, max_rounds=0)
+    out, cl, order = gsdr.cluster_fasta(data, threshold=0.90)
+    hout, hcl, horder = host_path(data, threshold=0.90)
+    np.testing.assert_array_equal(order, oorder)
+    np.testing.assert_array_equal(horder, oorder)
+    assert out == hout

@@ -108,9 +108,9 @@ def test_lcs_edge_lengths():
     rng = np.random.default_rng(7)
     seqs, pairs = [], []
     # lengths around word / lane / class boundaries, and N-containing patterns
-    for q in (1, 2, 15, 16, 17, 31, 32, 33, 63, 64, 65, 1023, 1024, 1025, 2048, 2049, 4096,
-              4097, 8192, 8193, 16384, 16385, 32768, 32769, 50000, 65536, 65537, 70000,
-              131072, 131073):
+    for q in (1, 2, 15, 16, 17, 31, 32, 33, 63, 64, 65, 1023, 1024, 1025, 2048, 2049, 3072,
+              3073, 4096, 4097, 5120, 5121, 6144, 6145, 7168, 7169, 8192, 8193, 16384, 16385,
+              32768, 32769, 50000, 65536, 65537, 70000, 131072, 131073):
         b = rand_seq(rng, q + int(rng.integers(0, 40)))
         a = mutate(rng, b[:q], 0.03)
         seqs.append(b)

@@ -33,6 +33,25 @@ def test_tie_order_matches_std_sort(tmp_path):
     assert not np.array_equal(stable, order)
 
 
+@pytest.mark.parametrize("mode", ["few", "lognormal"])
+def test_tie_order_matches_std_sort_large(tmp_path, mode):
+    # >= 65,536 records: the sort runs its independent parts on threads and
+    # must still give std::sort's permutation
+    rng = np.random.default_rng(1)
+    n = 120000
+    if mode == "few":
+        lens = rng.choice([20, 21, 22, 25], size=n)
+    else:
+        lens = np.clip(rng.lognormal(np.log(60), 0.5, size=n), 12, 300).astype(int)
+    base = rng.choice(list(b"ACGT"), int(lens.max())).tobytes()
+    data = b"".join(b">x%d\n" % i + base[:L] + b"\n" for i, L in enumerate(lens))
+    path = tmp_path / "ties_large.fa"
+    path.write_bytes(data)
+    order, _, _ = orc.run(str(path), None, t=0.99, d=1, max_rounds=0)
+    f = gsdr.read_file(str(path))
+    np.testing.assert_array_equal(f.order(), order)
+
+
 @pytest.mark.parametrize("data", [
     b"",
     b"ACGT\n>a\nAC\n",
