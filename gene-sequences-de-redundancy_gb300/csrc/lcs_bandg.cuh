@@ -18,6 +18,13 @@
 // frozen / initial-state rules of lcs_band.cuh, so the decision is exact for
 // the same reason: banded-LCS <= L' <= LCS and every path with >= c matches
 // lies in the band.
+//
+// Match masks: each lane keeps its window words' masks for the four base
+// codes in a per-warp table in shared memory (rebuilt from the bit planes
+// when the window slides, at most once per 32 bases), so a step of a block
+// that lies wholly inside every busy group's text reads one 16-byte entry
+// instead of forming four masks from the planes (block_full); a warp with a
+// group at the end of its text takes the plane path with the end mask.
 #pragma once
 #include <stdint.h>
 
@@ -55,6 +62,7 @@ __device__ __forceinline__ int group_sum(int v) {
 template <int G>
 struct BandGroup {
     static constexpr int W = kGroupWords;
+    static_assert(W == 4, "refresh() and the 16-byte table entries hold four words");
     uint32_t V[W], H[W], Lo[W];
     const uint32_t* pq;  // pattern, packed
     const uint32_t* pt;  // text, packed
@@ -65,11 +73,25 @@ struct BandGroup {
     int zf;              // zeros of the frozen words above the window
     int lane, j;         // lane in the warp, lane in the group
     uint32_t gmask;      // the group's lanes
+    uint4* tab;          // this lane's masks: tab[32 * code] (the warp's table + lane)
 
-    __device__ __forceinline__ void init_lane(int lane_) {
+    // wtab: the warp's 4 x 32 entries of shared memory (entry code * 32 + lane,
+    // so a quarter-warp's loads hit eight different 16-byte bank groups)
+    __device__ __forceinline__ void init_lane(int lane_, uint4* wtab) {
         lane = lane_;
         j = lane_ & (G - 1);
         gmask = G == 32 ? 0xffffffffu : ((1u << G) - 1u) << (lane_ & ~(G - 1));
+        tab = wtab + lane_;
+    }
+
+    // The masks of the four base codes for the window words held now.
+    __device__ __forceinline__ void refresh() {
+#pragma unroll
+        for (int code = 0; code < 4; code++) {
+            const uint32_t ch = (code & 2) ? 0xffffffffu : 0u, cl = (code & 1) ? 0xffffffffu : 0u;
+            tab[32 * code] = make_uint4(~((H[0] ^ ch) | (Lo[0] ^ cl)), ~((H[1] ^ ch) | (Lo[1] ^ cl)),
+                                        ~((H[2] ^ ch) | (Lo[2] ^ cl)), ~((H[3] ^ ch) | (Lo[3] ^ cl)));
+        }
     }
 
     __device__ __forceinline__ void load_word(int slot, int w) {
@@ -95,6 +117,7 @@ struct BandGroup {
             V[i] = 0xffffffffu;
             load_word(i, W * j + i);
         }
+        refresh();
     }
 
     // An idle group: no text, so every step leaves the state unchanged.
@@ -108,12 +131,18 @@ struct BandGroup {
     // One text base (ch / cl: its bits as full masks; vm all ones for a
     // real base, zero past the end of the text).
     __device__ __forceinline__ void step(uint32_t ch, uint32_t cl, uint32_t vm) {
-        uint32_t m[W], u[W], s[W];
+        uint32_t m[W];
 #pragma unroll
-        for (int i = 0; i < W; i++) {
-            m[i] = ~((H[i] ^ ch) | (Lo[i] ^ cl));
-            u[i] = V[i] & m[i] & vm;
-        }
+        for (int i = 0; i < W; i++) m[i] = ~((H[i] ^ ch) | (Lo[i] ^ cl));
+        step_masks(m, vm);
+    }
+
+    // The rest of a step once the match masks m are known (vm: all ones for a
+    // real base, zero past the end of the text).
+    __device__ __forceinline__ void step_masks(const uint32_t (&m)[W], uint32_t vm) {
+        uint32_t u[W], s[W];
+#pragma unroll
+        for (int i = 0; i < W; i++) u[i] = V[i] & m[i] & vm;
         uint32_t cy = 0;
         add4_carry(s[0], s[1], s[2], s[3], V[0], V[1], V[2], V[3], u[0], u[1], u[2], u[3], cy);
         const uint32_t all = s[0] & s[1] & s[2] & s[3];
@@ -124,6 +153,20 @@ struct BandGroup {
         add4_inc(s[0], s[1], s[2], s[3], cin);
 #pragma unroll
         for (int i = 0; i < W; i++) V[i] = s[i] | (V[i] & ~m[i]);
+    }
+
+    // 32 text bases that lie inside the text of every busy group of the warp
+    // (an idle group has V = 0, which any step leaves at 0): the masks come
+    // from the table, indexed by the base's code.
+    __device__ __forceinline__ void block_full(uint32_t tw0, uint32_t tw1) {
+#pragma unroll
+        for (int jj = 0; jj < 32; jj++) {
+            const uint32_t tw = jj < 16 ? tw0 : tw1;
+            const uint32_t code = (tw >> (30 - 2 * (jj & 15))) & 3u;
+            const uint4 mm = tab[32 * code];
+            const uint32_t m[W] = {mm.x, mm.y, mm.z, mm.w};
+            step_masks(m, 0xffffffffu);
+        }
     }
 
     // The 32 text bases x0 .. x0 + 31 (packed words tw0: x0 .. x0 + 15,
@@ -185,6 +228,7 @@ struct BandGroup {
                 H[W - 1] = nh;
                 Lo[W - 1] = nl;
             }
+            refresh();
         }
         return -1;
     }

@@ -711,8 +711,9 @@ __global__ void __launch_bounds__(kAlignThreads) k_bandg(DevReads R, RoundState*
     const unsigned lt_mask = (1u << lane) - 1u;
     const Pair* list = A.pairs + (size_t)cls * A.seg_cap;
     int* work = A.work + cls;
+    __shared__ uint4 btab[kAlignThreads / 32][4 * 32];  // match masks, per warp
     BandGroup<G> L;
-    L.init_lane(lane);
+    L.init_lane(lane, btab[threadIdx.x >> 5]);
     L.clear();
     Pair p{-1, -1};
     bool busy = false, more = true;
@@ -745,7 +746,9 @@ __global__ void __launch_bounds__(kAlignThreads) k_bandg(DevReads R, RoundState*
             if (L.x0 < L.T) tw0 = __ldg(L.pt + (L.x0 >> 4));
             if (L.x0 + 16 < L.T) tw1 = __ldg(L.pt + (L.x0 >> 4) + 1);
         }
-        L.block(tw0, tw1);
+        // a block inside every busy group's text takes the table path
+        if (__all_sync(kFull, !busy || L.x0 + 32 <= L.T)) L.block_full(tw0, tw1);
+        else L.block(tw0, tw1);
         const int d = L.finish_block(busy);
         if (busy && d >= 0) {
             if (leader) {
