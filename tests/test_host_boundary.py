@@ -33,13 +33,16 @@ def test_tie_order_matches_std_sort(tmp_path):
     assert not np.array_equal(stable, order)
 
 
-@pytest.mark.parametrize("mode", ["few", "lognormal"])
+@pytest.mark.parametrize("mode", ["two", "few", "lognormal"])
 def test_tie_order_matches_std_sort_large(tmp_path, mode):
-    # >= 65,536 records: the sort runs its independent parts on threads and
-    # must still give std::sort's permutation
+    # >= 65,536 records: the sort runs on a team of threads (partitions shared
+    # by the team, then parts from a stack) and must still give std::sort's
+    # permutation
     rng = np.random.default_rng(1)
     n = 120000
-    if mode == "few":
+    if mode == "two":
+        lens = rng.choice([30, 31], size=n)
+    elif mode == "few":
         lens = rng.choice([20, 21, 22, 25], size=n)
     else:
         lens = np.clip(rng.lognormal(np.log(60), 0.5, size=n), 12, 300).astype(int)
