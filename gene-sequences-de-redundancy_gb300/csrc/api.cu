@@ -341,7 +341,9 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     R_.threshold = opts.threshold;
     // band tiles of the banded alignment kernels (gsdr_opts; 0 = automatic,
     // where the environment may still override the defaults)
-    R_.band_serial = opts.band_serial > 0 ? opts.band_serial : opts.band_serial < 0 ? 0 : kBandMaxSerial;
+    R_.band_serial = opts.band_serial > 0   ? opts.band_serial
+                     : opts.band_serial < 0 ? 0
+                                            : kBandMaxSerial;
     if (opts.band_serial == 0)
         if (const char* bs = std::getenv("GSDR_BAND_SERIAL")) R_.band_serial = std::atoll(bs);
     R_.group_max_w = opts.group_words > 0 ? std::min(opts.group_words, kGroupMaxWords)

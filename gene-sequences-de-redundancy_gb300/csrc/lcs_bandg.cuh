@@ -88,9 +88,12 @@ struct BandGroup {
     __device__ __forceinline__ void refresh() {
 #pragma unroll
         for (int code = 0; code < 4; code++) {
-            const uint32_t ch = (code & 2) ? 0xffffffffu : 0u, cl = (code & 1) ? 0xffffffffu : 0u;
-            tab[32 * code] = make_uint4(~((H[0] ^ ch) | (Lo[0] ^ cl)), ~((H[1] ^ ch) | (Lo[1] ^ cl)),
-                                        ~((H[2] ^ ch) | (Lo[2] ^ cl)), ~((H[3] ^ ch) | (Lo[3] ^ cl)));
+            const uint32_t ch = (code & 2) ? 0xffffffffu : 0u;
+            const uint32_t cl = (code & 1) ? 0xffffffffu : 0u;
+            uint32_t m[W];
+#pragma unroll
+            for (int i = 0; i < W; i++) m[i] = ~((H[i] ^ ch) | (Lo[i] ^ cl));
+            tab[32 * code] = make_uint4(m[0], m[1], m[2], m[3]);
         }
     }
 
