@@ -253,3 +253,31 @@ def test_sycl_kmers_skip_windows_over_non_acgt():
             words[v] = words.get(v, 0) + 1
     assert dict(zip(w.tolist(), c.tolist())) == words
     assert sum(c) == 6
+
+
+def test_fasta_input_buffers():
+    # gsdr_cluster_fasta takes the FASTA bytes from bytes or from a contiguous
+    # uint8 array (for example a view of pinned host memory)
+    data = b">a\nACGT\n"
+    p1, n1 = gsdr._host_bytes(data)
+    arr = np.frombuffer(data, dtype=np.uint8).copy()
+    p2, n2 = gsdr._host_bytes(arr)
+    assert n1 == n2 == len(data)
+    assert p2.value == arr.ctypes.data
+    for bad in (np.zeros(4, dtype=np.int32), np.zeros((2, 2), dtype=np.uint8),
+                np.zeros(8, dtype=np.uint8)[::2]):
+        with pytest.raises(TypeError):
+            gsdr._host_bytes(bad)
+
+
+def test_tuned_opts_carry_every_setting():
+    from gsdr.autotune import TILES, tuned_opts
+
+    res = {"best": {"batch": 512, "word_filter": "index", "group_words": 64,
+                    "band_serial": 4096}}
+    o = tuned_opts(res, 0.9)
+    assert (o.batch, o.word_filter, o.group_words, o.band_serial) == (512, 2, 64, 4096)
+    assert abs(o.threshold - 0.9) < 1e-6
+    # every tile the tuner tries is a valid option
+    for gw, bs in TILES:
+        gsdr.resolve_opts(gsdr.default_opts(group_words=gw, band_serial=bs))
