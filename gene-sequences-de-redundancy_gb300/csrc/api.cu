@@ -15,6 +15,7 @@
 #include "gsdr.h"
 #include "gsdr_device.cuh"
 #include "gsdr_host.h"
+#include "nvtx_range.h"
 #include "gsdr_testing.h"
 #include "job.h"
 #include "lcs_band.cuh"
@@ -506,6 +507,7 @@ int Job::loop_timed() {
 
 int Job::run(int pass_limit) {
     if (n == 0) return GSDR_OK;
+    NvtxRange range_run("gsdr: job run");
     const double t0 = now_ms();
     const int k = opts.word_length;
     const bool drop = opts.drop == 1;
@@ -514,6 +516,7 @@ int Job::run(int pass_limit) {
     stats.filter_max_bytes = stats.filter_max_ms = 0;
     JCUDA(cudaSetDevice(opts.device));
     JCUDA(cudaEventRecord(ev_[1], stream));
+    NvtxRange range_prep("gsdr: preparation");
     // baseToNumber + compressData + createCutoff + createPrefix (func.cu:139-403)
     JCUDA(cudaMemsetAsync(R_.packed, 0, sizeof(uint32_t) * ((size_t)pack_off_[n] + 8), stream));
     if (R_.brk)
@@ -536,11 +539,14 @@ int Job::run(int pass_limit) {
         JCUDA(cudaGetLastError());
     }
     JCUDA(cudaEventRecord(ev_[2], stream));
+    range_prep.end();
     // clustering / clusteringDrop (func.cu:1001-1097)
     init_rounds(R_, B_, batched_ ? 1 : 0, r_max_, stream, pass_limit);
     stats.kernel_launches += 1;
     JCUDA(cudaGetLastError());
+    NvtxRange range_loop(batched_ ? "gsdr: batched passes" : "gsdr: rounds");
     int rc = opts.stage_timing ? loop_timed() : loop_graph();
+    range_loop.end();
     if (rc) return rc;
     JCUDA(cudaEventRecord(ev_[3], stream));
     JCUDA(cudaMemcpyAsync(h_state_, B_.st, sizeof(RoundState), cudaMemcpyDeviceToHost, stream));

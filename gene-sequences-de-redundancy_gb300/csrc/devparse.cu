@@ -32,6 +32,7 @@
 #include "gsdr.h"
 #include "gsdr_device.cuh"
 #include "gsdr_host.h"
+#include "nvtx_range.h"
 #include "job.h"
 #include "stdsort.h"
 
@@ -398,6 +399,7 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
             std::fprintf(stderr, "%s ms\n", line.c_str());
         }
     } tp{marks};
+    NvtxRange range_read("gsdr: FASTA bytes to reads (device parse, host sort)");
 
     // the file on the device, with room for multi-line records' data after it
     // (at most the file's size) and 16 bytes of slack for word loads
@@ -515,6 +517,7 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     }
     const double t_parse = now_ms();
     mark("sort");
+    range_read.end();
 
     // the clustering on the device-resident reads
     // (bytes: the device copy; the job reads only sizes from the view on the host)
@@ -530,6 +533,7 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     mark("run");
     if (rc) return rc;
     // the output records, formatted on the device
+    NvtxRange range_out("gsdr: output records");
     DevBuf d_order, sz;
     DCUDA(cudaMalloc(&d_order.p, sizeof(int32_t) * nr));
     DCUDA(cudaMalloc(&sz.p, sizeof(uint32_t) * (size_t)nr + 16));
