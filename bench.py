@@ -142,6 +142,20 @@ def key_figures():
     return out
 
 
+def libstdcxx_loaded():
+    """File name of the libstdc++ this process loaded (its version suffix):
+    the host sort reproduces std::sort's permutation with that library's own
+    introsort steps, so the version goes into the line."""
+    try:
+        with open("/proc/self/maps") as fh:
+            for ln in fh:
+                if "libstdc++" in ln:
+                    return os.path.realpath(ln.split()[-1]).rsplit("/", 1)[-1]
+    except OSError:
+        pass
+    return None
+
+
 def heaviest_launch(nbytes, ms, peak):
     """The filter launch that read the most input bytes in a stage-timed run:
     its bytes, event-timed duration and bandwidth against the HBM peak."""
@@ -185,8 +199,15 @@ def align_roofline(r, figures):
     """The alignment stage is integer-ALU bound (bit-parallel LCS): GCUPS over
     the full-DP cells of the pairs it decides, and the ALU pipe utilisation
     ncu measured for its dominant kernel."""
+    ms = r["align_ms"]
+    done = r.get("cells_computed") or 0.0
     return {"bound": "int_alu", "kernel": "k_align_single / k_align",
-            "gcups": r["gcups"], "stage_ms": r["align_ms"], "cells": r["stats"]["cells"],
+            "gcups": r["gcups"], "stage_ms": ms, "cells": r["stats"]["cells"],
+            "gcups_note": "cells = full-DP q x T of every aligned pair (the reference's DP "
+                          "work); early exits, bands and the greedy bound skip most of them",
+            "cells_computed": done,
+            "computed_over_full_dp": done / r["stats"]["cells"] if r["stats"]["cells"] else None,
+            "computed_gcups": done / (ms * 1e-3) / 1e9 if ms > 0 else None,
             "alu_pipe_pct_ncu": figures.get("align.alu_pipe_pct"),
             "ipc_ncu": figures.get("align.ipc")}
 
@@ -215,11 +236,12 @@ def oracle_lib():
 
 
 def cpu_run(data_path, t, threads):
+    """The oracle on a FASTA file: (seconds, sort permutation, cluster array)."""
     orc = oracle_lib()
     t0 = time.perf_counter()
     order, cl, st = orc.run(data_path, None, t=t, threads=threads)
     dt = time.perf_counter() - t0
-    return dt, len(cl), st
+    return dt, order, cl
 
 
 def write_workload(cfg, n_reads, seed, path):
@@ -235,73 +257,144 @@ def write_workload(cfg, n_reads, seed, path):
 SERVING_T = (0.80, 0.85, 0.90, 0.95, 1.00)
 
 
-def serving_run(args, device):
-    """A Poisson stream of clustering jobs through gsdr_server (continuous
-    batching, admission by device footprint): the serving workload's recipe
-    (jobs of the 10k-read recipe with lengths 150-5000 bp, threshold drawn from
-    0.80 .. 1.00) scaled so the stream takes seconds: sizes log-uniform over
-    1k-20k reads, and 300-1.5k reads with lengths up to 2,000 bp for the
-    alignment-only thresholds (t <= 0.879 turns the filters off, which makes a
-    job quadratic in its size).  t = 1.00 jobs are rejected as the reference
-    rejects them.  Job FASTA bytes are generated before the clock starts."""
+def _record_ends(data):
+    """Byte offset after each record of a single-line FASTA buffer."""
+    import numpy as np
+
+    a = np.frombuffer(data, dtype=np.uint8)
+    starts = np.flatnonzero(a == ord(">"))
+    return np.append(starts[1:], len(a))
+
+
+def serving_jobs(args):
+    """The serving workload's job stream: Poisson arrivals (args.serving_rate
+    per second), threshold uniform over 0.80 .. 1.00, jobs of the 10k-read
+    recipe with 150-5000 bp reads.  Jobs at t >= 0.88 (word filter on) draw
+    their size log-uniform over 1k-200k reads, as the recipe says; jobs at
+    t <= 0.879 turn the filters off (the reference's drop mode), which makes a
+    job quadratic in its size, so they draw 300-1.5k reads of at most 2000 bp.
+    A job of n reads is the first n records of one pre-generated file of the
+    recipe (records are in random order, so a prefix is a sample of it); t =
+    1.00 jobs are refused as the reference refuses them.  Returns (jobs as
+    (payload array, t, n), gaps in seconds, recipe text)."""
     import gsdr
     import numpy as np
 
     rng = np.random.default_rng(20261207)
+    big = gsdr.synth_fasta(4, n_reads=200000, seed=4100, n_seeds=40000, len_lo=150,
+                           len_hi=5000)
+    small = gsdr.synth_fasta(4, n_reads=1500, seed=4200, n_seeds=300, len_lo=150, len_hi=2000)
+    pools = {}
+    for key, data in (("filter", big), ("drop", small)):
+        pools[key] = (np.frombuffer(data, dtype=np.uint8), _record_ends(data))
     jobs = []
     for i in range(args.serving_jobs):
         t = float(SERVING_T[rng.integers(0, len(SERVING_T))])
         drop = t < 0.88
-        lo, hi = (300, 1500) if drop else (1000, 20000)
+        lo, hi = (300, 1500) if drop else (1000, 200000)
         n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
-        data = gsdr.synth_fasta(4, n_reads=n, seed=5000 + i, n_seeds=max(1, n // 5),
-                                len_lo=150, len_hi=2000 if drop else 5000)
-        jobs.append((data, t, n))
+        arr, ends = pools["drop" if drop else "filter"]
+        jobs.append((arr[: ends[n - 1]], t, n))
     gaps = rng.exponential(1.0 / args.serving_rate, len(jobs))
-    srv = gsdr.Server(device=device, max_inflight=4)
-    lat, reads, status = {}, {}, {}
-    t0 = time.perf_counter()
+    recipe = ("Poisson arrivals; jobs of the 10k-read recipe, 150-5000 bp, t in "
+              "{0.80,0.85,0.90,0.95,1.00}; sizes 1k-200k reads for t >= 0.88, 300-1.5k reads "
+              "of <= 2000 bp for t <= 0.879 (alignment only, quadratic); each job the first n "
+              "records of one generated file of the recipe")
+    return jobs, gaps, recipe
+
+
+def serve_stream(jobs, gaps, device, max_inflight):
+    """Submits the jobs at their arrival times (gaps None: all at once) and
+    waits for all.  Returns per-job (status, latency, run_ms, reads), wall s."""
+    import gsdr
+
+    srv = gsdr.Server(device=device, max_inflight=max_inflight)
+    lat, status, run = {}, {}, {}
     ids = []
+    t0 = time.perf_counter()
     try:
         due = t0
-        for (data, t, n), g in zip(jobs, gaps):
-            due += g
-            while True:
-                now = time.perf_counter()
-                if now >= due:
-                    break
-                r = srv.wait(int((due - now) * 1000) + 1)
-                if r:
-                    lat[r[0]], status[r[0]] = r[2], r[1]
-            jid = srv.submit(data, t)
-            ids.append(jid)
-            reads[jid] = n
+        for k, (data, t, n) in enumerate(jobs):
+            if gaps is not None:
+                due += gaps[k]
+                while True:
+                    now = time.perf_counter()
+                    if now >= due:
+                        break
+                    r = srv.wait(int((due - now) * 1000) + 1)
+                    if r:
+                        lat[r[0]], status[r[0]] = r[2], r[1]
+            ids.append((srv.submit(data, t), n))
         while len(lat) < len(ids):
             r = srv.wait(600000)
             if r is None:
                 break
             lat[r[0]], status[r[0]] = r[2], r[1]
-        t_end = time.perf_counter()
-        for jid in ids:
+        wall = time.perf_counter() - t0
+        for jid, _ in ids:
+            if jid in lat:
+                run[jid] = srv.times(jid)[1]
+        results = {jid: srv.result(jid)[1] for jid, _ in ids[:3] if status.get(jid) == 0}
+        for jid, _ in ids:
             if jid in lat:
                 srv.release(jid)
     finally:
         srv.close()
-    ok = [j for j in ids if status.get(j) == 0]
-    ls = np.array([lat[j] for j in ok]) if ok else np.array([0.0])
-    done_reads = sum(reads[j] for j in ok)
+    rows = [(status.get(j), lat.get(j), run.get(j), n) for j, n in ids]
+    return rows, wall, results
+
+
+def serving_run(args, device):
+    """The serving stream through gsdr_server (continuous batching: jobs
+    admitted by device footprint as slots free up, each on its own stream):
+    p50 / p99 job latency, aggregate sequences/s, and two measures of overlap
+    -- jobs running at once on average (sum of the jobs' run times over the
+    stream's wall time) and the same 32 jobs submitted at once with 1 slot
+    against 4 slots (wall-time ratio: > 1 means the device ran jobs side by
+    side).  The first jobs' results are checked against the oracle."""
+    import numpy as np
+
+    jobs, gaps, recipe = serving_jobs(args)
+    rows, wall, results = serve_stream(jobs, gaps, device, 4)
+    ok = [r for r in rows if r[0] == 0]
+    ls = np.array([r[1] for r in ok]) if ok else np.array([0.0])
+    busy = sum(r[2] for r in ok if r[2] is not None) / 1e3
+    done_reads = sum(r[3] for r in ok)
+    # overlap: 32 filter-mode jobs of the stream, all submitted at once
+    burst = [j for j in jobs if j[1] >= 0.88 and j[1] < 1.0][:32]
+    _, wall1, _ = serve_stream(burst, None, device, 1)
+    _, wall4, _ = serve_stream(burst, None, device, 4)
+    # a sample of served results against the oracle
+    checked, match = 0, True
+    try:
+        import tempfile
+
+        import oracle_binding
+
+        with tempfile.TemporaryDirectory() as td:
+            for k, cl in results.items():
+                data, t, n = jobs[k - 1]
+                if n > 20000:
+                    continue
+                _, ocl, _, _ = oracle_binding.run_bytes(data.tobytes(), td, t=t)
+                checked += 1
+                match = match and len(ocl) == len(cl) and bool((ocl == cl).all())
+    except Exception as e:  # the checker is optional here; say why it did not run
+        match = f"not checked: {e}"
     return {
-        "jobs": len(ids), "completed": len(ok),
-        "rejected_t1": sum(1 for j in ids if status.get(j) == 1),
-        "failed": sum(1 for j in ids if status.get(j) not in (0, 1)),
+        "jobs": len(rows), "completed": len(ok),
+        "rejected_t1": sum(1 for r in rows if r[0] == 1),
+        "failed": sum(1 for r in rows if r[0] not in (0, 1)),
         "arrival_rate_per_s": args.serving_rate,
         "p50_latency_ms": float(np.percentile(ls, 50)),
         "p99_latency_ms": float(np.percentile(ls, 99)),
-        "seqs_per_s": done_reads / (t_end - t0), "reads": done_reads,
-        "wall_s": t_end - t0, "max_inflight": 4,
-        "recipe": "Poisson arrivals; jobs of the 10k-read recipe, 150-5000 bp, t in "
-                  "{0.80,0.85,0.90,0.95,1.00}; sizes 1k-20k reads (300-1.5k, <= 2000 bp "
-                  "for t <= 0.879)",
+        "seqs_per_s": done_reads / wall, "reads": done_reads,
+        "wall_s": wall, "max_inflight": 4,
+        "mean_jobs_running": busy / wall if wall > 0 else None,
+        "burst": {"jobs": len(burst), "wall_s_1_slot": wall1, "wall_s_4_slots": wall4,
+                  "overlap_speedup": wall1 / wall4 if wall4 > 0 else None},
+        "oracle_checked": checked, "oracle_match": match,
+        "recipe": recipe,
     }
 
 
@@ -323,6 +416,14 @@ def combine_ranks(r, world):
     return r
 
 
+def config_line(args, n, t, world):
+    """The `config` object of both arms' lines (same keys, same values)."""
+    return {"workload": CONFIG_NAMES[args.config], "reads": n, "threshold": t,
+            "form": "plain" if args.batch == 1 else f"batched R={args.batch}",
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (sequence bytes + k-mer tables > 1 GB per step)"}
+
+
 def bench_reference(args, rank, world):
     """--impl reference: the oracle (CPU restatement) on the host cores."""
     if rank != 0:
@@ -335,7 +436,7 @@ def bench_reference(args, rank, world):
     t = CONFIG_T[args.config]
     times = []
     for i in range(args.warmup + args.steps):
-        dt, nr, st = cpu_run(path, t, threads)
+        dt, _, _ = cpu_run(path, t, threads)
         if i >= args.warmup:
             times.append(dt)
     os.unlink(path)
@@ -346,8 +447,7 @@ def bench_reference(args, rank, world):
         "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": CONFIG_NAMES[args.config], "reads": n, "threshold": t,
-                   "l2": "host run"},
+        "config": config_line(args, n, t, 1),
         "cpu_baseline": {"value": value, "unit": "seqs/s", "cores": threads, "kind": "port",
                          "sample": f"whole workload ({n} reads) per step; the reference has "
                                    "no CPU path, so its restatement (oracle) runs"},
@@ -392,6 +492,7 @@ def bench_ours(args, rank, world, local):
     clock_info = clocks.stop()
     cl_dev = job.cluster()
     job.close()
+    order_dev = f.order().copy()
 
     # e2e: FASTA bytes in host memory to output FASTA bytes in host memory
     # through gsdr_cluster_fasta (parse on the device, the host std::sort,
@@ -465,7 +566,8 @@ def bench_ours(args, rank, world, local):
         "align_ms": st_t.ms_align, "gcups": align_gcups,
         "peak": peak, "peak_kind": peak_kind, "t": t, "plain": plain,
         "word_index": st_t.word_index, "r_max": st_t.batch, "config": args.config,
-        "serving": serving, "autotune": tune,
+        "serving": serving, "autotune": tune, "cl_dev": cl_dev, "order_dev": order_dev,
+        "cells_computed": st_t.cells_computed,
     }
 
 
@@ -478,9 +580,11 @@ def main():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--reads", type=int, default=None)
     ap.add_argument("--seed", type=int, default=None)
-    ap.add_argument("--batch", type=int, default=0, help="0 = batched, adaptive R up to 256; 1 = plain")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="0 = batched with adaptive R (up to the job's R_max, 1024 by "
+                         "default); 1 = plain (one representative per round); R > 1 = R")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--serving-jobs", type=int, default=40,
+    ap.add_argument("--serving-jobs", type=int, default=200,
                     help="jobs in the serving stream (p50/p99 latency); 0 = skip")
     ap.add_argument("--serving-rate", type=float, default=20.0, help="job arrivals per second")
     ap.add_argument("--autotune", action="store_true",
@@ -530,6 +634,8 @@ def main():
     combine_ranks(r, world)
     if rank != 0:
         return
+    import numpy as np  # noqa: F401  (parity check below)
+
     n_total = r["n"] * world
     value = n_total / (r["ms_step"] * 1e-3)
     e2e = n_total / (r["e2e_ms"] * 1e-3)
@@ -562,10 +668,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic",
-        "config": {"workload": CONFIG_NAMES[args.config], "reads": r["n"], "threshold": r["t"],
-                   "form": "plain" if args.batch == 1 else f"batched R={args.batch}",
-                   "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (sequence bytes + k-mer tables > 1 GB per step)"},
+        "config": config_line(args, r["n"], r["t"], world),
         "e2e": {"value": e2e, "unit": "seqs/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"],
                 "path": "gsdr_cluster_fasta: FASTA bytes in pinned host memory -> output FASTA "
@@ -587,6 +690,7 @@ def main():
                                                "pairs_aligned", "pairs_accepted", "ms_prep",
                                                "ms_cluster", "word_index", "batch")},
         "device_result_matches_e2e": r["same"],
+        "host": {"libstdcxx": libstdcxx_loaded(), "cpu_cores": os.cpu_count()},
     }
     if not args.no_cpu:
         import tempfile
@@ -595,11 +699,20 @@ def main():
             path = os.path.join(td, "w.fa")
             n = write_workload(args.config, args.reads, args.seed, path)
             threads = os.cpu_count() or 1
-            dt, _, _ = cpu_run(path, r["t"], threads)
+            dt, order, ocl = cpu_run(path, r["t"], threads)
         line["cpu_baseline"] = {"value": n / dt, "unit": "seqs/s", "cores": threads,
                                 "kind": "port",
                                 "sample": f"whole workload ({n} reads), one run"}
+        # the oracle's result on the whole workload against the GPU's
+        same = (len(ocl) == len(r["cl_dev"]) and bool((ocl == r["cl_dev"]).all())
+                and bool((order == r["order_dev"]).all()))
+        line["parity_vs_oracle"] = same
+        line["parity_detail"] = {"reads": int(len(ocl)), "compared": "sort permutation and "
+                                 "cluster array of every read, oracle vs device run",
+                                 "representatives": int((ocl == np.arange(len(ocl))).sum())}
     print(json.dumps(line), flush=True)
+    if line.get("parity_vs_oracle") is False:
+        sys.exit("bench: the device result differs from the oracle's")
 
 
 if __name__ == "__main__":

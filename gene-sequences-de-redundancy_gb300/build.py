@@ -19,7 +19,7 @@ OUT = os.path.join(PKG, "_build")
 INC = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU = ["prep.cu", "rounds.cu", "api.cu", "noalloc.cu", "server.cu", "devparse.cu"]
+CU = ["prep.cu", "rounds.cu", "api.cu", "noalloc.cu", "server.cu", "devparse.cu", "devmem.cu"]
 CPP = ["fasta.cpp"]
 
 

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "devmem.h"
 #include "gsdr.h"
 #include "gsdr_device.cuh"
 #include "gsdr_host.h"
@@ -269,9 +270,10 @@ Job::~Job() {
     if (graph_) cudaGraphDestroy(graph_);
     for (auto& e : ev_)
         if (e) cudaEventDestroy(e);
-    if (dmem_) cudaFree(dmem_);
-    if (h_done_) cudaFreeHost(h_done_);
-    if (h_state_) cudaFreeHost(h_state_);
+    // back to the library's pool after this job's own work (no device-wide wait)
+    if (dmem_) dev_free(dmem_, stream);
+    pinned_release(h_done_);
+    pinned_release(h_state_);
     if (own_stream_ && stream) cudaStreamDestroy(stream);
 }
 
@@ -331,11 +333,13 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
         own_stream_ = true;
     }
     for (auto& e : ev_) JCUDA(cudaEventCreate(&e));
-    JCUDA(cudaMallocHost(&h_done_, sizeof(int32_t)));
-    JCUDA(cudaMallocHost(&h_state_, sizeof(RoundState)));
+    static_assert(sizeof(RoundState) <= kPinnedSlot, "round state exceeds a pinned slot");
+    h_done_ = static_cast<int32_t*>(pinned_slot());
+    h_state_ = static_cast<RoundState*>(pinned_slot());
+    if (!h_done_ || !h_state_) return fail(GSDR_ENOMEM, "pinned host memory");
     if (n == 0) return GSDR_OK;
     dbytes_ = carve_all(nullptr, n, n_bytes_, P, opts.drop == 1, opts.word_length, R_, B_);
-    JCUDA(cudaMalloc(&dmem_, dbytes_));
+    JCUDA(dev_alloc(&dmem_, dbytes_, stream));
     carve_all(reinterpret_cast<char*>(dmem_), n, n_bytes_, P, opts.drop == 1, opts.word_length,
               R_, B_);
     stats.word_index = P.idx_cap > 0 ? 1 : (P.bits ? 2 : 0);
@@ -569,6 +573,7 @@ int Job::run(int pass_limit) {
     stats.pairs_aligned = (int64_t)(h.cnt_aligned - h.cnt_pig_reject);
     stats.pairs_accepted = (int64_t)h.cnt_accepted;
     stats.cells = (double)h.cells;
+    stats.cells_computed = (double)h.cells_done;
     stats.filter_bytes = (double)h.filter_bytes;
     stats.ms_total = now_ms() - t0;
     return GSDR_OK;
@@ -834,6 +839,12 @@ int Job::lcs_pairs(const int32_t* pat, const int32_t* txt, int n_pairs, int mapp
 }
 
 }  // namespace gsdr
+
+extern "C" int gsdr_set_spin_limit(int32_t device, int32_t polls) {
+    if (cudaSetDevice(device) != cudaSuccess) return fail(GSDR_EDEVICE, "no such CUDA device");
+    if (set_spin_limit(polls)) return fail(GSDR_EDEVICE, "cannot set the spin limit");
+    return GSDR_OK;
+}
 
 extern "C" int gsdr_lcs_decide(const char* bytes, int64_t n_bytes, const int64_t* off,
                                const int32_t* len, int32_t n_seq, const int32_t* pat,

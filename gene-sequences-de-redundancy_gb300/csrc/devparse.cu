@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "gsdr.h"
+#include "devmem.h"
 #include "gsdr_device.cuh"
 #include "gsdr_host.h"
 #include "nvtx_range.h"
@@ -350,11 +351,15 @@ int grid_of(int64_t items, int per_block, int cap) {
     return (int)g;
 }
 
+// A device buffer from the library's pool, returned to it on the stream it
+// was taken on when the buffer goes out of scope (devmem.h).
 struct DevBuf {
+    cudaStream_t s;
     void* p = nullptr;
-    ~DevBuf() {
-        if (p) cudaFree(p);
-    }
+    explicit DevBuf(cudaStream_t st) : s(st) {}
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { dev_free(p, s); }
     template <class T>
     T* as() const {
         return reinterpret_cast<T*>(p);
@@ -403,8 +408,8 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
 
     // the file on the device, with room for multi-line records' data after it
     // (at most the file's size) and 16 bytes of slack for word loads
-    DevBuf file;
-    DCUDA(cudaMalloc(&file.p, (size_t)(2 * n + 64)));
+    DevBuf file(s);
+    DCUDA(dev_alloc(&file.p, (size_t)(2 * n + 64), s));
     DCUDA(cudaMemsetAsync(file.as<uint8_t>() + n, 0, 64, s));
     DCUDA(cudaMemcpyAsync(file.p, fasta, (size_t)n, cudaMemcpyHostToDevice, s));
     uint8_t* b = file.as<uint8_t>();
@@ -412,15 +417,15 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
 
     const int64_t n_chunks = (n + kChunk - 1) / kChunk;
     const int64_t per = (int64_t)kScanThreads * kScanItems;
-    DevBuf scan_tmp, small;
-    DCUDA(cudaMalloc(&scan_tmp.p, sizeof(uint32_t) * (size_t)(std::max<int64_t>(n_chunks, 1) / per + 2 +
-                                                              (n / per) + 2)));
-    DCUDA(cudaMalloc(&small.p, 64));
+    DevBuf scan_tmp(s), small(s);
+    DCUDA(dev_alloc(&scan_tmp.p, sizeof(uint32_t) * (size_t)(std::max<int64_t>(n_chunks, 1) / per + 2 +
+                                                              (n / per) + 2), s));
+    DCUDA(dev_alloc(&small.p, 64, s));
     uint32_t* d_total = small.as<uint32_t>();
     uint32_t h_total = 0;
 
-    DevBuf cnt;
-    DCUDA(cudaMalloc(&cnt.p, sizeof(uint32_t) * (size_t)std::max<int64_t>(n_chunks, 1)));
+    DevBuf cnt(s);
+    DCUDA(dev_alloc(&cnt.p, sizeof(uint32_t) * (size_t)std::max<int64_t>(n_chunks, 1), s));
     k_nl_count<<<grid_of(n_chunks, 8, 1 << 16), 256, 0, s>>>(b, n, n_chunks, cnt.as<uint32_t>());
     rc = scan_u32(cnt.as<uint32_t>(), cnt.as<uint32_t>(), n_chunks, scan_tmp.as<uint32_t>(), d_total,
                   s, &h_total);
@@ -428,14 +433,14 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     const int64_t n_nl = h_total;
     // getline: a last line without '\n' still counts; "a\n" is one line
     const int64_t n_lines = n_nl + (n > 0 && fasta[n - 1] != '\n' ? 1 : 0);
-    DevBuf nl;
-    DCUDA(cudaMalloc(&nl.p, sizeof(int64_t) * (size_t)std::max<int64_t>(n_nl, 1)));
+    DevBuf nl(s);
+    DCUDA(dev_alloc(&nl.p, sizeof(int64_t) * (size_t)std::max<int64_t>(n_nl, 1), s));
     k_nl_write<<<grid_of(n_chunks, 8, 1 << 16), 256, 0, s>>>(b, n, n_chunks, cnt.as<uint32_t>(),
                                                              nl.as<int64_t>());
 
-    DevBuf hdr, hdr_ex;
-    DCUDA(cudaMalloc(&hdr.p, sizeof(uint32_t) * (size_t)std::max<int64_t>(n_lines, 1)));
-    DCUDA(cudaMalloc(&hdr_ex.p, sizeof(uint32_t) * (size_t)std::max<int64_t>(n_lines, 1)));
+    DevBuf hdr(s), hdr_ex(s);
+    DCUDA(dev_alloc(&hdr.p, sizeof(uint32_t) * (size_t)std::max<int64_t>(n_lines, 1), s));
+    DCUDA(dev_alloc(&hdr_ex.p, sizeof(uint32_t) * (size_t)std::max<int64_t>(n_lines, 1), s));
     k_line_kind<<<grid_of(n_lines, 256, 1 << 16), 256, 0, s>>>(b, n, nl.as<int64_t>(), n_nl, n_lines,
                                                                 hdr.as<uint32_t>());
     rc = scan_u32(hdr.as<uint32_t>(), hdr_ex.as<uint32_t>(), n_lines, scan_tmp.as<uint32_t>(),
@@ -444,13 +449,13 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     const int64_t n_rec = 1 + (int64_t)h_total;
     if (n_rec > INT32_MAX) return fail(GSDR_EUNSUPPORTED, "too many records");
 
-    DevBuf head, name_off, name_len, data_off, data_len, pieces;
-    DCUDA(cudaMalloc(&head.p, sizeof(int64_t) * n_rec));
-    DCUDA(cudaMalloc(&name_off.p, sizeof(int64_t) * n_rec));
-    DCUDA(cudaMalloc(&name_len.p, sizeof(int32_t) * n_rec));
-    DCUDA(cudaMalloc(&data_off.p, sizeof(int64_t) * n_rec));
-    DCUDA(cudaMalloc(&data_len.p, sizeof(int64_t) * n_rec));
-    DCUDA(cudaMalloc(&pieces.p, sizeof(int32_t) * n_rec));
+    DevBuf head(s), name_off(s), name_len(s), data_off(s), data_len(s), pieces(s);
+    DCUDA(dev_alloc(&head.p, sizeof(int64_t) * n_rec, s));
+    DCUDA(dev_alloc(&name_off.p, sizeof(int64_t) * n_rec, s));
+    DCUDA(dev_alloc(&name_len.p, sizeof(int32_t) * n_rec, s));
+    DCUDA(dev_alloc(&data_off.p, sizeof(int64_t) * n_rec, s));
+    DCUDA(dev_alloc(&data_len.p, sizeof(int64_t) * n_rec, s));
+    DCUDA(dev_alloc(&pieces.p, sizeof(int32_t) * n_rec, s));
     if (n_lines == 0) {
         // an empty file: one record with an empty name and no data
         DCUDA(cudaMemsetAsync(head.p, 0, sizeof(int64_t), s));
@@ -534,26 +539,26 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     if (rc) return rc;
     // the output records, formatted on the device
     NvtxRange range_out("gsdr: output records");
-    DevBuf d_order, sz;
-    DCUDA(cudaMalloc(&d_order.p, sizeof(int32_t) * nr));
-    DCUDA(cudaMalloc(&sz.p, sizeof(uint32_t) * (size_t)nr + 16));
+    DevBuf d_order(s), sz(s);
+    DCUDA(dev_alloc(&d_order.p, sizeof(int32_t) * nr, s));
+    DCUDA(dev_alloc(&sz.p, sizeof(uint32_t) * (size_t)nr + 16, s));
     DCUDA(cudaMemcpyAsync(d_order.p, res->order.data(), sizeof(int32_t) * nr,
                           cudaMemcpyHostToDevice, s));
     const DevReads& R = job.device_reads();
     k_out_sizes<<<grid_of(nr, 256, 1 << 14), 256, 0, s>>>(job.device_cluster(), d_order.as<int32_t>(),
                                                          name_len.as<int32_t>(), R.len, nr,
                                                          sz.as<uint32_t>());
-    DevBuf sz_off;
-    DCUDA(cudaMalloc(&sz_off.p, sizeof(uint32_t) * (size_t)nr + 16));
+    DevBuf sz_off(s);
+    DCUDA(dev_alloc(&sz_off.p, sizeof(uint32_t) * (size_t)nr + 16, s));
     rc = scan_u32(sz.as<uint32_t>(), sz_off.as<uint32_t>(), nr, scan_tmp.as<uint32_t>(), d_total, s,
                   &h_total);
     if (rc) return rc;
     // (the output is smaller than the file, so 32-bit offsets hold for files
     // below 4 GiB; larger outputs are formatted on the host)
-    DevBuf outd;
+    DevBuf outd(s);
     const int64_t out_bytes = h_total;
     if (n < ((int64_t)1 << 32)) {
-        DCUDA(cudaMalloc(&outd.p, (size_t)out_bytes + 16));
+        DCUDA(dev_alloc(&outd.p, (size_t)out_bytes + 16, s));
         k_out_copy<<<grid_of(nr, 8, 1 << 16), 256, 0, s>>>(
             b, job.device_cluster(), d_order.as<int32_t>(), name_off.as<int64_t>(),
             name_len.as<int32_t>(), R.off, R.len, sz_off.as<uint32_t>(), nr, outd.as<uint8_t>(), 0);

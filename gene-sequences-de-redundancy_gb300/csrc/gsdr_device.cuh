@@ -139,6 +139,10 @@ struct RoundState {
     unsigned long long cnt_pig_reject;  // pairs the pigeon filter removed
     unsigned long long cells;
     unsigned long long filter_bytes;
+    // DP cells the alignment kernels stepped: per block of 32 text bases, the
+    // 32-bit pattern (or band window) words a warp or lane held x 32 bits x 32
+    // bases; early exits and bands make it smaller than `cells`
+    unsigned long long cells_done;
 };
 
 // ---- prep.cu ----
@@ -193,6 +197,10 @@ struct RoundBuffers {
 };
 void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
                  int pass_limit = 0);
+// Polls each bounded wait of the alignment kernels makes on the current
+// device before it gives up (polls < 0: the default, kSpinLimit); for tests
+// that make a wait run out.  Returns 0 or -1 (CUDA error).
+int set_spin_limit(int polls);
 // One plain round (filter, align, compact, advance); `parity` picks which
 // remain buffer is the input.  `count` accumulates kernel launches; `ev4`
 // (optional) receives events around the filter and alignment stages.

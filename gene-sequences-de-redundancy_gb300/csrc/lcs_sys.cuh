@@ -29,7 +29,7 @@
 //   reject  Z(q-R) + min(R, q) < c, R = bases after X, Z(i) = zeros below
 //           pattern position i: any common subsequence has <= Z(i) matches
 //           with text[0..X] and <= min(q-i, R) after, maximal at i = q-R.
-// Every wait is bounded (kSpinLimit polls) and reports an error instead of
+// Every wait is bounded (c_spin_limit polls) and reports an error instead of
 // hanging.
 //
 // Chunk mode (patterns above one group's 65,536 rows): the pattern is cut into
@@ -50,6 +50,9 @@ constexpr int kSysRing = 4;     // carry words in flight between two warps
 constexpr int kSysZRing = 16;   // checkpoints kept per warp
 constexpr int kSysCk = 4;       // blocks of 32 bases between checkpoints
 constexpr int kSpinLimit = 1 << 22;
+// Polls a wait makes before it gives up: kSpinLimit unless a test lowered it
+// (set_spin_limit, rounds.cu); with 0 every wait gives up at once.
+static __constant__ int c_spin_limit = kSpinLimit;
 
 // Shared state of a group of up to NW warps deciding one pair.
 template <int NW>
@@ -77,7 +80,7 @@ __device__ __forceinline__ void group_bar(int id, int nthreads) {
 }
 
 __device__ __forceinline__ bool spin_until_ge(const int* p, int target, const int* stop) {
-    for (int it = 0; it < kSpinLimit; it++) {
+    for (int it = 0; it < c_spin_limit; it++) {
         if (vload(p) >= target) return true;
         if (vload(stop)) return true;
         if (it > 64) __nanosleep(20);
@@ -167,14 +170,15 @@ __host__ __device__ constexpr int sys_peq_words(int W) { return 5 * W * 32; }
 
 // The decision of one pair on B warps of a group (gw = this warp's index).
 // The result lands in S.result (1 accept, 0 reject) once the group meets at
-// its barrier; S.error is set if a wait gave up.  peq: this warp's
+// its barrier; S.error is set if a wait gave up.  Returns the blocks of 32
+// steps this warp ran (its computed cells: blocks x 32 x 32 lanes x W x 32).  peq: this warp's
 // sys_peq_words(W) words of shared memory for the pattern's match masks.
 // Chunk mode (chunk true): gcin (or null for the first chunk) holds the
 // carry-in words of warp 0's lane 0, gcout (or null for the last chunk)
 // receives the carry-out words of the last warp's lane 31 (a full chunk), and
 // S.result is the chunk's zero count at the end of the text.
 template <int W, class Group>
-__device__ void lcs_sys_pair(Group& S, uint32_t* peq, const uint32_t* __restrict__ pq, int q,
+__device__ int lcs_sys_pair(Group& S, uint32_t* peq, const uint32_t* __restrict__ pq, int q,
                              const uint32_t* __restrict__ pt, int T, int c, int B, int gw,
                              int lane, int* err_flag, bool chunk = false,
                              const uint32_t* __restrict__ gcin = nullptr,
@@ -200,16 +204,17 @@ __device__ void lcs_sys_pair(Group& S, uint32_t* peq, const uint32_t* __restrict
     uint32_t from = 0;   // carry from lane l-1 at the previous step
     uint32_t wprev = 0;  // top lane: carry bits of the word being completed
     bool decided = false;
+    int blocks = 0;
     for (int m = 0; m < M; m++) {
-        if (vload(&S.stop)) return;
+        if (vload(&S.stop)) return blocks;
         uint32_t cin_word = 0;
         if (gw == 0 && gcin) cin_word = __ldcg(gcin + m);
         if (gw > 0) {
             if (!spin_until_ge(&S.ready[gw - 1], m + 1, &S.stop)) {
                 sys_fail(S, err_flag, lane);
-                return;
+                return blocks;
             }
-            if (vload(&S.stop)) return;
+            if (vload(&S.stop)) return blocks;
             __threadfence_block();
             cin_word = *(volatile uint32_t*)&S.carries[gw - 1][m % kSysRing];
             __syncwarp();
@@ -248,6 +253,7 @@ __device__ void lcs_sys_pair(Group& S, uint32_t* peq, const uint32_t* __restrict
                                            not_lane0, -1, lane);
         }
         __syncwarp();
+        blocks++;
         const bool last_block = m == M - 1;
         // end of text: final zero counts, published before the last carry word
         if (last_block) {
@@ -271,7 +277,7 @@ __device__ void lcs_sys_pair(Group& S, uint32_t* peq, const uint32_t* __restrict
                 }
                 if (!spin_until_ge(&S.consumed[gw], widx + 1 - kSysRing, &S.stop)) {
                     sys_fail(S, err_flag, lane);
-                    return;
+                    return blocks;
                 }
                 if (lane == 0) S.carries[gw][widx % kSysRing] = k2 == 0 ? wdone : wlast;
                 __threadfence_block();
@@ -314,7 +320,7 @@ __device__ void lcs_sys_pair(Group& S, uint32_t* peq, const uint32_t* __restrict
                 }
             }
         }
-        if (decided) return;
+        if (decided) return blocks;
     }
     if (gw == B - 1) {
         int zt = 0;
@@ -325,6 +331,7 @@ __device__ void lcs_sys_pair(Group& S, uint32_t* peq, const uint32_t* __restrict
             vstore(&S.stop, 1);
         }
     }
+    return blocks;
 }
 
 }  // namespace gsdr

@@ -12,10 +12,13 @@
 // In host code `g_scratch` names a host-side stand-in, not the device array:
 // its device address is fetched with cudaGetSymbolAddress once per device (on
 // the first call made with that device current) and that address is what the
-// kernels receive.  The first call on a device should therefore come before
-// any stream capture.  Every call reuses the same array, so each call first
+// kernels receive.  Every call reuses the same array, so each call first
 // clears what must start at zero; two calls that overlap on the GPU (other
-// streams, other host threads) race on it and give undefined results.
+// streams, other host threads) race on it and give undefined results.  Each
+// call reads two status words back and waits for its stream, so it returns
+// with the stream idle and cannot be made while that stream is capturing.
+// The address is kept for the life of the process: after a cudaDeviceReset
+// of a device, the array's address there is not looked up again.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -82,14 +85,23 @@ __global__ void k_na_init(RoundState* st, int* work, int32_t* cluster, int32_t* 
     }
 }
 
-// Queues every pair in the alignment class of its pattern's length.
-__global__ void k_na_bucket(RoundState* st, Pair* pairs, const int32_t* __restrict__ len_gf,
+// Queues every pair in the alignment class of its pattern's length.  An index
+// outside [0, n_seq), a pattern that appears in two pairs or a pattern longer
+// than the limit sets the invalid-input flag instead (the call then fails).
+__global__ void k_na_bucket(RoundState* st, Pair* pairs, int32_t* cluster,
+                            const int32_t* __restrict__ len_gf,
                             const int32_t* __restrict__ pat, const int32_t* __restrict__ txt,
                             int n_pairs, int n_seq) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_pairs;
          k += gridDim.x * blockDim.x) {
         const int p = pat[k], x = txt[k];
         if (p < 0 || p >= n_seq || x < 0 || x >= n_seq) {
+            st->pair_overflow = 1;
+            continue;
+        }
+        // one pair per pattern: the pattern's decision slot goes from -1
+        // (cleared) to -2 (claimed); a second claim finds it taken
+        if (atomicCAS(cluster + p, -1, -2) != -1) {
             st->pair_overflow = 1;
             continue;
         }
@@ -105,11 +117,17 @@ __global__ void k_na_bucket(RoundState* st, Pair* pairs, const int32_t* __restri
     }
 }
 
+// accept[k] = 1 iff the alignment stage joined pattern pat[k] to text txt[k];
+// a pair with an index outside [0, n_seq) reads nothing and gets 0 (the call
+// reports it as invalid input).
 __global__ void k_na_finish(const int32_t* __restrict__ cluster, const int32_t* __restrict__ pat,
-                            const int32_t* __restrict__ txt, int n_pairs, uint8_t* accept) {
+                            const int32_t* __restrict__ txt, int n_pairs, int n_seq,
+                            uint8_t* accept) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_pairs;
-         k += gridDim.x * blockDim.x)
-        accept[k] = cluster[pat[k]] == txt[k] ? 1 : 0;
+         k += gridDim.x * blockDim.x) {
+        const int p = pat[k];
+        accept[k] = (p >= 0 && p < n_seq && cluster[p] == txt[k]) ? 1 : 0;
+    }
 }
 
 }  // namespace
@@ -154,16 +172,21 @@ extern "C" int gsdr_lcs_decide_noalloc(const uint32_t* d_packed, const int64_t* 
     B.cluster = reinterpret_cast<int32_t*>(base + kOffCluster);
     int* work = reinterpret_cast<int*>(B.st + 1);
 
+    // an error left by the caller's own earlier work is theirs: report it
+    // without clearing it, before launching anything
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return fail(GSDR_EDEVICE, "noalloc: a CUDA error is pending from earlier work");
     const int threads = 256;
     const int grid = (n_seq > n_pairs ? n_seq : n_pairs) / threads + 1;
     k_na_init<<<grid < 1024 ? grid : 1024, threads, 0, s>>>(B.st, work, B.cluster, R.cut_base,
                                                            d_len_raw, n_seq, t);
-    k_na_bucket<<<(n_pairs + threads - 1) / threads, threads, 0, s>>>(B.st, B.pairs, d_len_gf,
-                                                                      d_pat, d_txt, n_pairs, n_seq);
+    k_na_bucket<<<(n_pairs + threads - 1) / threads, threads, 0, s>>>(
+        B.st, B.pairs, B.cluster, d_len_gf, d_pat, d_txt, n_pairs, n_seq);
     launch_align_stage(R, B, false, false, s);
     k_na_finish<<<(n_pairs + threads - 1) / threads, threads, 0, s>>>(B.cluster, d_pat, d_txt,
-                                                                      n_pairs, d_accept);
-    cudaError_t e = cudaGetLastError();
+                                                                      n_pairs, n_seq, d_accept);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return fail(GSDR_EDEVICE, cudaGetErrorString(e));
     // the flags of the state say whether every pair was valid and every wait ended
     int flags[2] = {0, 0};
@@ -172,7 +195,7 @@ extern "C" int gsdr_lcs_decide_noalloc(const uint32_t* d_packed, const int64_t* 
         e = cudaMemcpyAsync(&flags[1], &B.st->error, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(GSDR_EDEVICE, cudaGetErrorString(e));
-    if (flags[0]) return fail(GSDR_EINVAL, "noalloc: bad index or pattern longer than 32768 bases");
+    if (flags[0]) return fail(GSDR_EINVAL, "noalloc: index out of range, pattern in more than one pair, or pattern longer than 32768 bases");
     if (flags[1]) return fail(GSDR_ETIMEOUT, "noalloc: a device-side wait gave up");
     return GSDR_OK;
 }

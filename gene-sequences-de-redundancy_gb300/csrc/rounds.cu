@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
         S.result = 0;
         S.error = 0;
     }
-    unsigned long long acc = 0, cells = 0;
+    unsigned long long acc = 0, cells = 0, done = 0;
     while (true) {
         if (gw == 0 && lane == 0) S.idx = atomicAdd(A.work + cls, 1);
         group_bar(bar_id, bar_n);
@@ -523,9 +523,10 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
             const int words = (q + 31) >> 5;
             const int B = (words + 32 * W - 1) / (32 * W);
             if (gw < B)
-                lcs_sys_pair<W>(S, peq_all + warp * sys_peq_words(W),
-                                R.packed + R.pack_off[p.cand], q, R.packed + R.pack_off[p.rep], T,
-                                c, B, gw, lane, &st->error);
+                done += (unsigned long long)lcs_sys_pair<W>(
+                            S, peq_all + warp * sys_peq_words(W), R.packed + R.pack_off[p.cand],
+                            q, R.packed + R.pack_off[p.rep], T, c, B, gw, lane, &st->error) *
+                        (32ull * 32 * 32 * W);
         }
         group_bar(bar_id, bar_n);
         if (gw == 0 && lane == 0) {
@@ -549,6 +550,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
         if (!BATCH) atomicAdd(&st->cnt_accepted, acc);
         atomicAdd(&st->cells, cells);
     }
+    if (lane == 0 && done) atomicAdd(&st->cells_done, done);
 }
 
 // The four single-warp classes of the batched grouping (1x1, 1x2, 1x4, 1x8)
@@ -572,6 +574,7 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, R
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     SysGroupT<1>& S = groups[warp];
     unsigned long long cells = 0;
+    unsigned done = 0;  // blocks of 32 steps x words per lane this warp ran
     while (true) {
         int i = 0;
         if (lane == 0) i = atomicAdd(work, 1);
@@ -600,16 +603,18 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, R
             // each over the warp), not the class's power of two -- a step
             // costs about three integer ops per word plus three
             const int wl = (q + 1023) >> 10;  // 1..8 in these classes (q <= 8192)
+            int blocks = 0;
             switch (wl) {
-                case 1: lcs_sys_pair<1>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 2: lcs_sys_pair<2>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 3: lcs_sys_pair<3>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 4: lcs_sys_pair<4>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 5: lcs_sys_pair<5>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 6: lcs_sys_pair<6>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                case 7: lcs_sys_pair<7>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
-                default: lcs_sys_pair<8>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 1: blocks = lcs_sys_pair<1>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 2: blocks = lcs_sys_pair<2>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 3: blocks = lcs_sys_pair<3>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 4: blocks = lcs_sys_pair<4>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 5: blocks = lcs_sys_pair<5>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 6: blocks = lcs_sys_pair<6>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                case 7: blocks = lcs_sys_pair<7>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
+                default: blocks = lcs_sys_pair<8>(S, peq, pq, q, pt, T, c, 1, 0, lane, &st->error); break;
             }
+            done += (unsigned)blocks * (unsigned)(wl > 8 ? 8 : wl);
             __syncwarp();
             ok = *(volatile int*)&S.error ? 0 : *(volatile int*)&S.result;
         }
@@ -619,6 +624,8 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align_single(DevReads R, R
         }
     }
     if (lane == 0 && cells) atomicAdd(&st->cells, cells);
+    // cells: 32 steps x 32 lanes x words per lane x 32 bits per block
+    if (lane == 0 && done) atomicAdd(&st->cells_done, (unsigned long long)done * (32ull * 32 * 32));
 }
 
 // Banded alignment (lcs_band.cuh) of the pairs of band class cls, whose band
@@ -644,7 +651,7 @@ __global__ void __launch_bounds__(kAlignThreads) k_band(DevReads R, RoundState* 
     Pair p{-1, -1};
     bool busy = false, more = true;
     unsigned long long cells = 0;
-    unsigned acc = 0;
+    unsigned acc = 0, done = 0;  // done: blocks of 32 text bases this lane ran on a pair
     while (true) {
         // lanes without a pair take the next ones (one atomic per warp)
         unsigned need = __ballot_sync(kFull, !busy);
@@ -678,6 +685,7 @@ __global__ void __launch_bounds__(kAlignThreads) k_band(DevReads R, RoundState* 
 #pragma unroll 1
         for (int j0 = 0; j0 < 32; j0 += G) L.template steps<G>(j0 < 16 ? tw0 : tw1, j0);
         if (busy) {
+            done++;
             const int d = L.finish_block();
             if (d >= 0) {
                 cells += (unsigned long long)L.T * (unsigned long long)L.q;
@@ -693,6 +701,8 @@ __global__ void __launch_bounds__(kAlignThreads) k_band(DevReads R, RoundState* 
     acc = (unsigned)warp_sum_i((int)acc);
     if (!BATCH && lane == 0 && acc) atomicAdd(&st->cnt_accepted, (unsigned long long)acc);
     if (cells) atomicAdd(&st->cells, cells);
+    // cells: 32 bases x the window's W words x 32 bits per block
+    if (done) atomicAdd(&st->cells_done, (unsigned long long)done * (32ull * 32 * W));
 }
 
 // Banded alignment (lcs_bandg.cuh) of the pairs of group class cls: one pair
@@ -712,6 +722,8 @@ __global__ void __launch_bounds__(kAlignThreads) k_bandg(DevReads R, RoundState*
     const Pair* list = A.pairs + (size_t)cls * A.seg_cap;
     int* work = A.work + cls;
     __shared__ uint4 btab[kAlignThreads / 32][4 * 32];  // match masks, per warp
+    __shared__ unsigned s_done[kAlignThreads / 32];  // blocks of 32 bases run by busy groups
+    if (lane == 0) s_done[threadIdx.x >> 5] = 0;
     BandGroup<G> L;
     L.init_lane(lane, btab[threadIdx.x >> 5]);
     L.clear();
@@ -750,6 +762,10 @@ __global__ void __launch_bounds__(kAlignThreads) k_bandg(DevReads R, RoundState*
         if (__all_sync(kFull, !busy || L.x0 + 32 <= L.T)) L.block_full(tw0, tw1);
         else L.block(tw0, tw1);
         const int d = L.finish_block(busy);
+        {
+            const unsigned ran = __ballot_sync(kFull, busy && leader);
+            if (lane == 0) s_done[threadIdx.x >> 5] += __popc(ran);
+        }
         if (busy && d >= 0) {
             if (leader) {
                 cells += (unsigned long long)L.T * (unsigned long long)L.q;
@@ -765,6 +781,10 @@ __global__ void __launch_bounds__(kAlignThreads) k_bandg(DevReads R, RoundState*
     acc = (unsigned)warp_sum_i((int)acc);
     if (!BATCH && lane == 0 && acc) atomicAdd(&st->cnt_accepted, (unsigned long long)acc);
     if (cells) atomicAdd(&st->cells, cells);
+    // cells: 32 bases x the window's 4G words x 32 bits per block
+    if (lane == 0 && s_done[threadIdx.x >> 5])
+        atomicAdd(&st->cells_done,
+                  (unsigned long long)s_done[threadIdx.x >> 5] * (32ull * 32 * 4 * G));
 }
 
 // Pairs whose pattern has more rows than one group of 8 warps x 32 lanes x 8
@@ -789,7 +809,7 @@ __global__ void __launch_bounds__(kAlignThreads, 1) k_align_long(DevReads R, Rou
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t* buf0 = carry + (size_t)blockIdx.x * 2 * carry_words;
     uint32_t* buf1 = buf0 + carry_words;
-    unsigned long long acc = 0, cells = 0;
+    unsigned long long acc = 0, cells = 0, done = 0;
     while (true) {
         if (threadIdx.x == 0) s_idx = atomicAdd(A.work + kLongClass, 1);
         __syncthreads();
@@ -822,9 +842,11 @@ __global__ void __launch_bounds__(kAlignThreads, 1) k_align_long(DevReads R, Rou
                 const uint32_t* cin = k > 0 ? ((k & 1) ? buf0 : buf1) : nullptr;
                 uint32_t* cout = k + 1 < nch ? ((k & 1) ? buf1 : buf0) : nullptr;
                 if (warp < B)
-                    lcs_sys_pair<8>(S, peq_all + warp * sys_peq_words(8),
-                                    pq + (size_t)k * (kChunkRows / 16), qk, pt, T, c, B, warp,
-                                    lane, &st->error, true, cin, cout);
+                    done += (unsigned long long)lcs_sys_pair<8>(
+                                S, peq_all + warp * sys_peq_words(8),
+                                pq + (size_t)k * (kChunkRows / 16), qk, pt, T, c, B, warp, lane,
+                                &st->error, true, cin, cout) *
+                            (32ull * 32 * 32 * 8);
                 __syncthreads();
                 err = *(volatile int*)&S.error != 0;
                 ztot += *(volatile int*)&S.result;
@@ -844,6 +866,7 @@ __global__ void __launch_bounds__(kAlignThreads, 1) k_align_long(DevReads R, Rou
         if (!BATCH && acc) atomicAdd(&st->cnt_accepted, acc);
         if (cells) atomicAdd(&st->cells, cells);
     }
+    if (lane == 0 && done) atomicAdd(&st->cells_done, done);
 }
 
 __global__ void k_compact(RoundState* st, const int32_t* __restrict__ remain_in,
@@ -2130,6 +2153,11 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
 bool index_in_smem(int k, int r_max, int64_t cap, int smem_optin) {
     if (cap <= 0 || cap >= 65536) return false;
     return IndexSmem(k, r_max, cap, true).bytes(1024 / 32) <= smem_optin;
+}
+
+int set_spin_limit(int polls) {
+    const int v = polls < 0 ? kSpinLimit : polls;
+    return cudaMemcpyToSymbol(c_spin_limit, &v, sizeof(int)) == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace gsdr

@@ -33,7 +33,7 @@ struct ServerJob {
     int64_t id = 0;
     std::vector<char> fasta;
     float threshold = 0.95f;
-    double t_submit = 0, t_done = 0;
+    double t_submit = 0, t_start = 0, t_done = 0;
     int status = GSDR_OK;
     std::string error;
     gsdr_fasta* parsed = nullptr;
@@ -71,6 +71,7 @@ struct gsdr_server {
 namespace {
 
 void run_job(gsdr_server* s, std::shared_ptr<ServerJob> j) {
+    j->t_start = now_ms();
     gsdr_opts o;
     gsdr_default_opts(&o);
     o.threshold = j->threshold;
@@ -265,6 +266,19 @@ int gsdr_server_result(gsdr_server* s, int64_t job, char* buf, int64_t cap, int6
         std::memcpy(buf, j->out.data(), j->out.size());
     }
     if (cluster) std::memcpy(cluster, j->cluster.data(), j->cluster.size() * sizeof(int32_t));
+    return GSDR_OK;
+}
+
+int gsdr_server_times(gsdr_server* s, int64_t job, double* queued_ms, double* run_ms) {
+    if (!s) return fail(GSDR_EINVAL, "server: null server");
+    std::lock_guard<std::mutex> lock(s->mu);
+    auto it = s->jobs.find(job);
+    if (it == s->jobs.end()) return fail(GSDR_ENOTFOUND, "server: unknown job");
+    const ServerJob& j = *it->second;
+    if (j.t_done == 0) return fail(GSDR_EBUSY, "server: job not finished");
+    const double start = j.t_start > 0 ? j.t_start : j.t_done;  // refused before running
+    if (queued_ms) *queued_ms = start - j.t_submit;
+    if (run_ms) *run_ms = j.t_done - start;
     return GSDR_OK;
 }
 

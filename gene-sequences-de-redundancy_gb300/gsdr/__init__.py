@@ -21,6 +21,9 @@ SYNTH_PATH = os.path.join(BUILD_DIR, "libgsdr_synth.so")
 CLI_PATH = os.path.join(BUILD_DIR, "cluster")
 
 OK, EINVAL, ENOMEM, EDEVICE, ETIMEOUT, EIO, EUNSUPPORTED, EBUSY, ENOTFOUND = range(9)
+# limits of gsdr_lcs_decide_noalloc (include/gsdr.h)
+NOALLOC_MAX_PAIRS = 16384
+NOALLOC_MAX_SEQS = 65536
 
 
 class GsdrError(RuntimeError):
@@ -81,6 +84,7 @@ class Stats(C.Structure):
         ("word_index", C.c_int32),
         ("filter_max_bytes", C.c_double),
         ("filter_max_ms", C.c_double),
+        ("cells_computed", C.c_double),
     ]
 
     def as_dict(self):
@@ -171,6 +175,9 @@ def lib():
         L.gsdr_lcs_decide_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                               C.c_float, C.c_void_p, C.c_void_p]
+        L.gsdr_set_spin_limit.argtypes = [C.c_int32, C.c_int32]
+        L.gsdr_server_times.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double)]
         L.gsdr_server_create.argtypes = [C.POINTER(ServerOpts), C.POINTER(C.c_void_p)]
         L.gsdr_server_submit.argtypes = [C.c_void_p, C.c_char_p, C.c_int64, C.c_float,
                                          C.POINTER(C.c_int64)]
@@ -492,6 +499,12 @@ def lcs_decide_noalloc(d_packed, d_pack_off, d_len_raw, d_len_gf, n_seq, d_pat, 
                                          d_pat, d_txt, n_pairs, C.c_float(t), d_accept, stream))
 
 
+def set_spin_limit(polls, device=0):
+    """gsdr_set_spin_limit: polls each bounded device-side wait of the
+    alignment kernels makes before giving up (None or < 0: the default)."""
+    _check(lib().gsdr_set_spin_limit(device, -1 if polls is None else int(polls)))
+
+
 class Server:
     """Continuous batching of clustering jobs on one GPU (gsdr_server_*)."""
 
@@ -501,10 +514,16 @@ class Server:
         _check(lib().gsdr_server_create(C.byref(so), C.byref(h)))
         self._h = h
 
-    def submit(self, fasta: bytes, threshold: float) -> int:
+    def submit(self, fasta, threshold: float) -> int:
+        """Queues a job: FASTA as bytes or a contiguous uint8 array (copied by
+        the server); returns its id."""
         j = C.c_int64()
-        _check(lib().gsdr_server_submit(self._h, fasta, len(fasta), C.c_float(threshold),
-                                        C.byref(j)))
+        if isinstance(fasta, np.ndarray):
+            a = np.ascontiguousarray(fasta, dtype=np.uint8)
+            ptr, n = C.cast(a.ctypes.data, C.c_char_p), a.size
+        else:
+            ptr, n = fasta, len(fasta)
+        _check(lib().gsdr_server_submit(self._h, ptr, n, C.c_float(threshold), C.byref(j)))
         return j.value
 
     def wait(self, timeout_ms=-1):
@@ -525,6 +544,12 @@ class Server:
         _check(lib().gsdr_server_result(self._h, job, buf, need.value, C.byref(need),
                                         cl.ctypes.data, C.byref(n)))
         return buf.raw[: need.value], cl[: n.value]
+
+    def times(self, job):
+        """(queued_ms, run_ms) of a finished job (gsdr_server_times)."""
+        q, r = C.c_double(), C.c_double()
+        _check(lib().gsdr_server_times(self._h, job, C.byref(q), C.byref(r)))
+        return q.value, r.value
 
     def release(self, job):
         _check(lib().gsdr_server_release(self._h, job))

@@ -105,6 +105,10 @@ typedef struct {
     double filter_max_bytes;  /* with stage_timing only: input bytes of the filter launch
                                  that read the most, and its time (filter_max_ms) */
     double filter_max_ms;
+    double cells_computed;    /* DP cells the alignment kernels actually stepped: per block
+                                 of 32 text bases, the 32-bit pattern or band-window words
+                                 a warp or lane held x 32 bits x 32 bases (early exits,
+                                 bands and the greedy bound make it smaller than cells) */
 } gsdr_stats;
 
 /* Fill `o` with the reference defaults (t 0.95, derived k/drop, pigeon 0). */
@@ -215,13 +219,20 @@ void gsdr_job_free(gsdr_job* job);
  * past its last base word), the raw length (for the cutoff ceil(len * t)) and
  * gap-free length of each sequence, and n_pairs (pattern, text) index pairs.
  * A pattern index may appear in at most one pair.  Output: d_accept[k] = 1 iff
- * LCS(pattern, text) >= ceil(raw length of the pattern * t).
+ * LCS(pattern, text) >= ceil(raw length of the pattern * t).  An index outside
+ * [0, n_seq), a pattern index in two pairs or a pattern above 32768 gap-free
+ * bases makes the call return GSDR_EINVAL (no out-of-range access is made).
  *
  * The first call on a device, made with that device current, looks up the
- * array's device address; make that first call before any stream capture.
- * Every call reuses the same array and clears what it needs at the start, so
- * calls that overlap on the GPU race and give undefined results.  The call
- * returns after the work on `stream` (a cudaStream_t, or NULL) has finished. */
+ * array's device address and keeps it for the life of the process (a
+ * cudaDeviceReset of that device is not followed).  Every call reuses the same
+ * array and clears what it needs at the start, so calls that overlap on the
+ * GPU (other streams, other host threads) race and give undefined results:
+ * the caller serialises them.  Each call reads its status back and waits for
+ * `stream` (a cudaStream_t, or NULL): it returns with that stream idle, and it
+ * must not be called while the stream is being captured.  A CUDA error still
+ * pending from the caller's earlier work is reported (GSDR_EDEVICE) and left
+ * in place, before anything is launched. */
 #define GSDR_NOALLOC_MAX_PAIRS 16384
 #define GSDR_NOALLOC_MAX_SEQS 65536
 int gsdr_lcs_decide_noalloc(const uint32_t* d_packed, const int64_t* d_pack_off,
@@ -261,6 +272,11 @@ int gsdr_server_wait(gsdr_server* s, int64_t timeout_ms, int64_t* job, int32_t* 
  * receives the size) and the cluster array in sorted order (may be NULL). */
 int gsdr_server_result(gsdr_server* s, int64_t job, char* buf, int64_t cap, int64_t* need,
                        int32_t* cluster, int32_t* n_reads);
+/* Timing of a finished job: submission to the start of its run on a worker
+ * (parse, sort, admission wait) and the run itself (device work and output
+ * formatting), host wall clock.  The sum of run_ms over jobs divided by the
+ * stream's wall time is the number of jobs running at once on average. */
+int gsdr_server_times(gsdr_server* s, int64_t job, double* queued_ms, double* run_ms);
 int gsdr_server_release(gsdr_server* s, int64_t job);
 void gsdr_server_destroy(gsdr_server* s);
 

@@ -33,6 +33,16 @@ int gsdr_lcs_decide(const char* bytes, int64_t n_bytes, const int64_t* off, cons
  * the early, full-size passes of a job (gsdr/autotune.py). */
 int gsdr_job_run_limited(gsdr_job* job, int32_t max_passes, gsdr_stats* stats);
 
+/* Polls each bounded wait of the alignment kernels (a warp of a multi-warp
+ * group waiting for its neighbour's carry words) makes on `device` before it
+ * gives up, sets the error flag and returns; polls < 0 restores the default
+ * (4,194,304).  With 0 every such wait gives up at once, so a call whose pairs
+ * need a multi-warp group returns GSDR_ETIMEOUT: the way tests check that a
+ * wait that runs out ends in a status and not in a hang.  The reference has no
+ * device-side waits (its errors are read once by checkError,
+ * cuda-version/func.cu:1118-1123). */
+int gsdr_set_spin_limit(int32_t device, int32_t polls);
+
 #ifdef __cplusplus
 }
 #endif

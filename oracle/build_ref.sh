@@ -4,8 +4,8 @@
 # infrastructure only: it produces the golden outputs of tests/golden/.
 #
 #   oracle/build_ref.sh stage   copy main.cu, func.cu, func.h from the reference
-#                               tree (read-only, $GSDR_REFERENCE, default
-#                               /root/reference) into oracle/_ref/src/
+#                               tree (read-only; its root in $GSDR_REFERENCE)
+#                               into oracle/_ref/src/
 #   oracle/build_ref.sh build   nvcc them for sm_103a into oracle/_ref/cluster_ref_<L>
 #                               for each MAX_LENGTH L given in $GSDR_REF_MAXLEN
 #
@@ -16,9 +16,10 @@ set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
 out="$here/_ref"
 src="$out/src"
-ref="${GSDR_REFERENCE:-/root/reference}"
+ref="${GSDR_REFERENCE:-}"
 case "${1:-build}" in
   stage)
+    [ -n "$ref" ] || { echo "set GSDR_REFERENCE to the reference tree's root" >&2; exit 2; }
     mkdir -p "$src"
     for f in main.cu func.cu func.h; do
       cp "$ref/cuda-version/$f" "$src/$f"

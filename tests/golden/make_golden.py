@@ -11,7 +11,7 @@ tests/golden/reference_outputs.json (or the path given as argument).
 With case names, only those cases run and their entries are merged into the
 existing output file.
 
-    python tests/golden/make_golden.py --results
+    GSDR_REFERENCE=<reference tree> python tests/golden/make_golden.py --results
 
 copies the reference's own output files (cuda-version/result.fasta and the
 SYCL program's top-level result.fasta) into tests/golden/ as
@@ -47,11 +47,15 @@ def ref_binary(max_len):
     raise RuntimeError(f"no reference build for reads of {max_len} bases")
 
 
-REFERENCE = "/root/reference"
+# root of the reference tree (read-only), for --results only
+REFERENCE = os.environ.get("GSDR_REFERENCE", "")
 
 
 def copy_results():
     import gzip
+
+    if not REFERENCE:
+        raise SystemExit("set GSDR_REFERENCE to the reference tree's root")
 
     for src, dst in (("cuda-version/result.fasta", "ref_cuda_result.fasta.gz"),
                      ("result.fasta", "ref_sycl_result.fasta.gz")):

@@ -112,6 +112,35 @@ def lcs(a: np.ndarray, b: np.ndarray, mode=1) -> int:
     return lib().orc_lcs(a.ctypes.data, len(a), b.ctypes.data, len(b), mode)
 
 
+def gap_free_codes(s: bytes) -> np.ndarray:
+    """ACGT/U (either case) -> 0..3 with every other byte dropped (the
+    reference's packing, cuda-version/func.cu:139-179, 272-299)."""
+    lut = np.full(256, 255, dtype=np.uint8)
+    for i, ch in enumerate(b"ACGT"):
+        lut[ch] = i
+        lut[ch | 0x20] = i
+    lut[ord("U")] = lut[ord("u")] = 3
+    c = lut[np.frombuffer(s, dtype=np.uint8)]
+    return c[c < 4]
+
+
+def lcs_decisions(seqs, pairs, t):
+    """The alignment-stage decision of kernel_align (cuda-version/func.cu:828-999)
+    for each (pattern, text) pair: 1 iff the gap-free LCS reaches the pattern's
+    base cutoff ceil(len * t) (func.cu:331-332)."""
+    lens = np.array([len(s) for s in seqs], dtype=np.int32)
+    _, base, _ = cutoffs(lens, t, 6)
+    out = []
+    for p, x in pairs:
+        a = gap_free_codes(seqs[p])
+        b = gap_free_codes(seqs[x])
+        if len(b) == 0:
+            out.append(0)
+            continue
+        out.append(1 if lcs(a, b) >= base[p] else 0)
+    return np.array(out, dtype=np.uint8)
+
+
 def pack(seq: bytes):
     out = np.zeros(len(seq) // 16 + 2, dtype=np.uint32)
     gaps = C.c_int()

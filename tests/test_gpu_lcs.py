@@ -35,29 +35,8 @@ def mutate(rng, s, rate, indel=0.2):
     return bytes(out)
 
 
-def gap_free_codes(s: bytes) -> np.ndarray:
-    """ACGT -> 0..3 with every other byte dropped (the reference's packing)."""
-    lut = np.full(256, 255, dtype=np.uint8)
-    for i, ch in enumerate(b"ACGT"):
-        lut[ch] = i
-        lut[ch | 0x20] = i
-    lut[ord("U")] = lut[ord("u")] = 3
-    c = lut[np.frombuffer(s, dtype=np.uint8)]
-    return c[c < 4]
-
-
 def expected(seqs, pairs, t):
-    lens = np.array([len(s) for s in seqs], dtype=np.int32)
-    _, base, _ = orc.cutoffs(lens, t, 6)
-    out = []
-    for p, x in pairs:
-        a = gap_free_codes(seqs[p])
-        b = gap_free_codes(seqs[x])
-        if len(b) == 0:
-            out.append(0)
-            continue
-        out.append(1 if orc.lcs(a, b) >= base[p] else 0)
-    return np.array(out, dtype=np.uint8)
+    return orc.lcs_decisions(seqs, pairs, t)
 
 
 def build_case(rng, n_pairs, qlen, tlen, kind):
