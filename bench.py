@@ -466,12 +466,20 @@ def bench_ours(args, rank, world, local):
     n = f.n
     opts = gsdr.default_opts(threshold=t, device=device, batch=args.batch)
     tune = None
-    if args.autotune:
-        from gsdr.autotune import autotune, tuned_opts
+    if args.autotune and args.batch == 0:
+        # the library's autotuner times the knobs on the job's first
+        # representatives and stores the winner in the tuning cache; the
+        # automatic job below (batch 0) then takes it from there by itself
+        from gsdr.autotune import autotune
 
-        tune = autotune(data, t, device=device)
-        if tune["best"]:
-            opts = tuned_opts(tune, t, device=device)
+        t_tune = time.perf_counter()
+        rep = autotune(data, t, device=device)
+        auto = [x for x in rep["trials"] if x.get("stage") == "R x form" and x.get("batch") == 0
+                and x.get("word_filter") == 0 and "us_per_rep" in x]
+        tune = {"best": rep["best"], "trials": len(rep["trials"]), "bucket": rep["bucket"],
+                "gpu": rep["gpu"], "cache": rep["cache"], "reps_timed": rep["reps"],
+                "automatic_us_per_rep": auto[0]["us_per_rep"] if auto else None,
+                "seconds": time.perf_counter() - t_tune}
     h2d = f.view.n_bytes + n * 8 + n * 4 + 2 * (n + 1) * 8
     d2h = n * 4
 
@@ -587,9 +595,11 @@ def main():
     ap.add_argument("--serving-jobs", type=int, default=200,
                     help="jobs in the serving stream (p50/p99 latency); 0 = skip")
     ap.add_argument("--serving-rate", type=float, default=20.0, help="job arrivals per second")
-    ap.add_argument("--autotune", action="store_true",
-                    help="choose R_max and the word filter's form by timing them on a "
-                         "sample of the workload (gsdr.autotune) before the timed runs")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the autotuner (by default gsdr_autotune times R_max, the word "
+                         "filter's form, band tiles, block shape and staging depth on the "
+                         "job's first representatives before the timed runs, and the timed "
+                         "automatic job takes the result from the tuning cache)")
     ap.add_argument("--stage-run", action="store_true",
                     help="one stage-timed clustering of the workload (CUDA events around "
                          "every filter and alignment launch; with GSDR_TRACE=1 a line per "
@@ -688,7 +698,8 @@ def main():
         "autotune": r["autotune"],
         "stats": {k: r["stats"][k] for k in ("rounds", "passes", "pairs_prefilter", "pairs_word",
                                                "pairs_aligned", "pairs_accepted", "ms_prep",
-                                               "ms_cluster", "word_index", "batch")},
+                                               "ms_cluster", "word_index", "batch",
+                                               "tuned")},
         "device_result_matches_e2e": r["same"],
         "host": {"libstdcxx": libstdcxx_loaded(), "cpu_cores": os.cpu_count()},
     }

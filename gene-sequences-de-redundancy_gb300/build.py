@@ -19,7 +19,8 @@ OUT = os.path.join(PKG, "_build")
 INC = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU = ["prep.cu", "rounds.cu", "api.cu", "noalloc.cu", "server.cu", "devparse.cu", "devmem.cu"]
+CU = ["prep.cu", "rounds.cu", "api.cu", "noalloc.cu", "server.cu", "devparse.cu", "devmem.cu",
+      "autotune.cu"]
 CPP = ["fasta.cpp"]
 
 

@@ -291,12 +291,14 @@ int64_t Job::footprint(const gsdr_reads* reads, const gsdr_opts* opts) {
 int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s) {
     int rc = validate(reads, opts_in, opts);
     if (rc) return rc;
+    const bool tuned = use_tune_cache && reads->n > 0 && apply_tuned(reads, opts);
     n = reads->n;
     n_bytes_ = reads->n_bytes;
     std::memset(&stats, 0, sizeof(stats));
     stats.k = opts.word_length;
     stats.drop = opts.drop;
     stats.pigeon = opts.pigeon;
+    stats.tuned = tuned ? 1 : 0;
     // word lengths 8..12 run one representative per round (the batched
     // filters keep the 4^k k-mer space on chip)
     batched_ = opts.batch != 1 && !(opts.drop == 0 && opts.word_length >= kWideK);
@@ -304,6 +306,13 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
         const char* tr = std::getenv("GSDR_TRACE");
         trace_ = tr && tr[0] == '1';
     }
+    if (tuned && trace_)
+        std::fprintf(stderr,
+                     "gsdr trace: knobs from the tuning cache: batch %d word_filter %d "
+                     "group_words %d band_serial %d align_blocks %d filter_blocks %d "
+                     "graph_steps %d\n",
+                     opts.batch, opts.word_filter, opts.group_words, opts.band_serial,
+                     opts.align_blocks, opts.filter_blocks, opts.graph_steps);
     Plan P;
     rc = make_plan(reads, opts, P);
     if (rc) return rc;
@@ -351,6 +360,8 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
                                             : kBandMaxSerial;
     if (opts.band_serial == 0)
         if (const char* bs = std::getenv("GSDR_BAND_SERIAL")) R_.band_serial = std::atoll(bs);
+    R_.align_blocks = opts.align_blocks;
+    R_.filter_blocks = opts.filter_blocks;
     R_.group_max_w = opts.group_words > 0 ? std::min(opts.group_words, kGroupMaxWords)
                                           : opts.group_words < 0 ? 0 : kGroupMaxWords;
     if (opts.group_words == 0)
@@ -398,7 +409,8 @@ void Job::launch_step(int parity, long long* count, cudaEvent_t* ev4) {
 
 int Job::capture_graph() {
     if (gexec_) return GSDR_OK;
-    const int unroll = batched_ ? 4 : 16;  // steps per graph launch; even, so the remain buffers alternate
+    // steps per graph launch (the staging depth); even, so the remain buffers alternate
+    const int unroll = opts.graph_steps > 0 ? opts.graph_steps : (batched_ ? 4 : 16);
     JCUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed));
     long long per = 0;
     for (int r = 0; r < unroll; r++) launch_step(r & 1, &per, nullptr);

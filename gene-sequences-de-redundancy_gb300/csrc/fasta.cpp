@@ -347,6 +347,11 @@ int gsdr_resolve_opts(gsdr_opts* o, const char** msg) {
         m = "band_serial must be -1, 0 or positive";
     } else if (o->group_words < -1 || o->group_words > 128) {
         m = "group_words must be -1..128";
+    } else if (o->align_blocks < 0 || o->align_blocks > 8 || o->filter_blocks < 0 ||
+               o->filter_blocks > 8) {
+        m = "align_blocks and filter_blocks must be 0..8";
+    } else if (o->graph_steps < 0 || o->graph_steps > 64 || (o->graph_steps & 1)) {
+        m = "graph_steps must be 0 or even, 2..64";
     } else if (o->variant == 1 && o->word_length != 0 &&
                (o->word_length < 4 || o->word_length > 8)) {
         m = "word length out of range (4<=word length<=8)";  // func.cpp:47-51

@@ -92,6 +92,10 @@ struct DevReads {
     // largest serial work (text bases x window words) of a pair given to the
     // lane-per-pair banded kernel; longer pairs go to the systolic kernels
     int64_t band_serial;
+    // block shape (gsdr_opts): resident CTAs per SM the alignment and the
+    // word-filter kernels are launched with (0: as many as fit)
+    int32_t align_blocks;
+    int32_t filter_blocks;
     // widest window (words) given to the group-banded kernel (kGroupMaxWords;
     // 0: none, those pairs go to the systolic kernels)
     int32_t group_max_w;

@@ -40,6 +40,9 @@ public:
     gsdr_stats stats{};
     int n = 0;
     cudaStream_t stream = nullptr;
+    // automatic jobs (batch 0) take the tuning cache's knobs for their
+    // workload bucket (autotune.cu); the autotuner's own trials do not
+    bool use_tune_cache = true;
 
 private:
     int plan_and_alloc();
@@ -66,5 +69,10 @@ private:
     DevReads R_{};
     RoundBuffers B_{};
 };
+
+// autotune.cu: the tuning cache's knobs for this workload's bucket on this
+// GPU, applied to every knob `o` leaves automatic (only when o.batch == 0);
+// true when the cache held the bucket.
+bool apply_tuned(const gsdr_reads* reads, gsdr_opts& o);
 
 }  // namespace gsdr

@@ -185,24 +185,49 @@ __global__ void __launch_bounds__(kFilterThreads, 6) k_filter(DevReads R, RoundS
     unsigned n_pf = 0, n_wf = 0, n_al = 0;
     unsigned long long bytes = 0;
     const int nwarps = gridDim.x * (kFilterThreads / 32);
-    for (int idx = blockIdx.x * (kFilterThreads / 32) + (threadIdx.x >> 5); idx < n;
-         idx += nwarps) {
-        const int q = remain[idx];
+    // Software pipeline over this warp's candidates: while candidate i is
+    // decided, the scalars of candidate i+1 (composition, cutoffs) are already
+    // in flight and the index of candidate i+2 too, so the chain of dependent
+    // loads (remain -> scalars -> list) overlaps the previous candidate's
+    // list stream instead of stalling the warp once per candidate.
+    int idx = blockIdx.x * (kFilterThreads / 32) + (threadIdx.x >> 5);
+    int q_nx = idx < n ? __ldg(remain + idx) : -1;
+    int q_af = idx + nwarps < n ? __ldg(remain + idx + nwarps) : -1;
+    int4 comp_nx = make_int4(0, 0, 0, 0);
+    int cb_nx = 0;
+    if (q_nx >= 0) {
+        comp_nx = R.comp[q_nx];
+        cb_nx = R.cut_base[q_nx];
+    }
+    for (; idx < n; idx += nwarps) {
+        const int q = q_nx;
+        const int4 comp_q = comp_nx;
+        const int cb_q = cb_nx;
+        // issue the next candidate's loads before this one's work
+        q_nx = q_af;
+        q_af = idx + 2 * nwarps < n ? __ldg(remain + idx + 2 * nwarps) : -1;
+        if (q_nx >= 0) {
+            comp_nx = R.comp[q_nx];
+            cb_nx = R.cut_base[q_nx];
+        }
         if (q == rep) continue;
         n_pf++;
         bytes += kCandFixedBytes;  // composition, cutoffs, index
         // kernel_preFilter (func.cu:738-754); lossless, so also used in drop mode.
-        if (!prefilter_pass(crep, R.comp[q], R.cut_base[q] - R.strict)) continue;
+        if (!prefilter_pass(crep, comp_q, cb_q - R.strict)) continue;
         if (!DROP) {
             // kernel_filter (func.cu:803-826): S = sum over distinct k-mers of
             // min(count in representative, count in candidate), compared with
             // the candidate's word cutoff.
             n_wf++;
             const int cw = R.cut_word[q];
+            const int64_t koff = R.kmer_off[q];
+            const int nk = R.n_kmer[q];
             bool decided = false, pass = false;
             if (BITS) {
                 // D = shared k-mers (non-zero counts) bounds S: D <= S <= D + min(excesses)
                 bytes += 4ull * NBW;
+                const int q_extra = R.kextra[q];
                 const uint4 cb = __ldcs(reinterpret_cast<const uint4*>(R.kbits + (size_t)q * NBW) + lane % (NBW / 4));
                 int d = 0;
                 if (lane < NBW / 4) {
@@ -212,11 +237,11 @@ __global__ void __launch_bounds__(kFilterThreads, 6) k_filter(DevReads R, RoundS
                 }
                 d = warp_sum_i(d);
                 if (d >= cw) decided = pass = true;
-                else if (d + min(R.kextra[q], rep_extra) < cw) decided = true;
+                else if (d + min(q_extra, rep_extra) < cw) decided = true;
             }
             if (!decided) {
-                const int ne4 = (R.n_kmer[q] + 3) >> 2;
-                const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + R.kmer_off[q]);
+                const int ne4 = (nk + 3) >> 2;
+                const uint4* e4 = reinterpret_cast<const uint4*>(R.kmer + koff);
                 bytes += 16ull * ne4;
                 int sum = 0;
 #pragma unroll 4
@@ -1831,6 +1856,13 @@ int grid_for(KernelT kernel, int threads, int smem, int cap_per_sm) {
     return num_sms() * per_sm;
 }
 
+// The job's block shape: a grid of at most `blocks` CTAs per SM (0: the full
+// grid, every CTA that fits).  The kernels loop over their work, so any grid
+// size gives the same result.
+int shaped(int grid, int blocks) {
+    return blocks > 0 ? min(grid, num_sms() * blocks) : grid;
+}
+
 // tent: null for a plain round; the batched form's tentatives otherwise (the
 // kernel then runs only in a pass with a single tentative).
 template <int K, bool DROP>
@@ -1844,7 +1876,7 @@ void launch_filter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain, 
                                  smem);
         grid = grid_for(k_filter<K, DROP>, kFilterThreads, smem, 8);
     }
-    k_filter<K, DROP><<<grid, kFilterThreads, smem, s>>>(R, B.st, remain, B.pairs, B.seg_cap,
+    k_filter<K, DROP><<<shaped(grid, R.filter_blocks), kFilterThreads, smem, s>>>(R, B.st, remain, B.pairs, B.seg_cap,
                                                          tent);
 }
 
@@ -1861,7 +1893,7 @@ void launch_bfilter_tab_t(const DevReads& R, RoundBuffers& B, const int32_t* rem
         cudaFuncSetAttribute(k_bfilter_tab<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         grid = grid_for(k_bfilter_tab<K>, kTabThreads, smem, 2);
     }
-    k_bfilter_tab<K><<<grid, kTabThreads, smem, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap);
+    k_bfilter_tab<K><<<shaped(grid, R.filter_blocks), kTabThreads, smem, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap);
 }
 
 template <int K, bool DROP>
@@ -1871,7 +1903,7 @@ void launch_bfilter_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
     } else {
         static int grid = 0;
         if (!grid) grid = grid_for(k_bprefilter, kFilterThreads, 0, 8);
-        k_bprefilter<<<grid, kFilterThreads, 0, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap);
+        k_bprefilter<<<shaped(grid, R.filter_blocks), kFilterThreads, 0, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap);
     }
 }
 
@@ -1900,12 +1932,12 @@ void launch_bfilter_idx_t(const DevReads& R, RoundBuffers& B, const int32_t* rem
                                                 B.idx_off16, B.idx_post16, (long long)B.idx_cap);
     if (in_smem) {
         const int grid = grid_for(k_bfilter_idx<K, true>, threads, fsmem, 2);
-        k_bfilter_idx<K, true><<<grid, threads, fsmem, s>>>(
+        k_bfilter_idx<K, true><<<shaped(grid, R.filter_blocks), threads, fsmem, s>>>(
             R, B.st, remain, B.tent, B.idx_off, B.idx_post, B.idx_off16, B.idx_post16, B.r_max,
             (long long)B.idx_cap, B.pairs, B.seg_cap);
     } else {
         const int grid = grid_for(k_bfilter_idx<K, false>, threads, fsmem, 8);
-        k_bfilter_idx<K, false><<<grid, threads, fsmem, s>>>(
+        k_bfilter_idx<K, false><<<shaped(grid, R.filter_blocks), threads, fsmem, s>>>(
             R, B.st, remain, B.tent, B.idx_off, B.idx_post, nullptr, nullptr, B.r_max,
             (long long)B.idx_cap, B.pairs, B.seg_cap);
     }
@@ -1921,9 +1953,9 @@ void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* re
         grid = grid_for(k_bfilter_bits<K>, kFilterThreads, 0, 8);
         xgrid = grid_for(k_bexact<K>, kFilterThreads, xsmem, 8);
     }
-    k_bfilter_bits<K><<<grid, kFilterThreads, 0, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap,
+    k_bfilter_bits<K><<<shaped(grid, R.filter_blocks), kFilterThreads, 0, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap,
                                                       B.amb);
-    k_bexact<K><<<xgrid, kFilterThreads, xsmem, s>>>(R, B.st, B.amb, B.pairs, B.seg_cap);
+    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kFilterThreads, xsmem, s>>>(R, B.st, B.amb, B.pairs, B.seg_cap);
 }
 
 template <bool BATCH>
@@ -1933,7 +1965,7 @@ void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain
         static int grid = 0;
         if (!grid) grid = grid_for(k_filter_g, kFilterThreads, 0, 8);
         k_gtab<<<64, 256, 0, s>>>(R, B.st, 0);
-        k_filter_g<<<grid, kFilterThreads, 0, s>>>(R, B.st, remain, B.pairs, B.seg_cap);
+        k_filter_g<<<shaped(grid, R.filter_blocks), kFilterThreads, 0, s>>>(R, B.st, remain, B.pairs, B.seg_cap);
         k_gtab<<<64, 256, 0, s>>>(R, B.st, 1);
         return;
     }
@@ -1998,21 +2030,21 @@ void launch_align_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s)
                              smem);
         grid = grid_for(k_align<G, W, BATCH>, kAlignThreads, smem, 8);
     }
-    k_align<G, W, BATCH><<<grid, kAlignThreads, smem, s>>>(R, B.st, align_args(B), cls);
+    k_align<G, W, BATCH><<<shaped(grid, R.align_blocks), kAlignThreads, smem, s>>>(R, B.st, align_args(B), cls);
 }
 
 template <int G, bool BATCH>
 void launch_bandg_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
     static int grid = 0;
     if (!grid) grid = grid_for(k_bandg<G, BATCH>, kAlignThreads, 0, 8);
-    k_bandg<G, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
+    k_bandg<G, BATCH><<<shaped(grid, R.align_blocks), kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
 }
 
 template <int W, bool BATCH>
 void launch_band_t(const DevReads& R, RoundBuffers& B, int cls, cudaStream_t s) {
     static int grid = 0;
     if (!grid) grid = grid_for(k_band<W, BATCH>, kAlignThreads, 0, 8);
-    k_band<W, BATCH><<<grid, kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
+    k_band<W, BATCH><<<shaped(grid, R.align_blocks), kAlignThreads, 0, s>>>(R, B.st, align_args(B), cls);
 }
 
 template <bool BATCH>
@@ -2063,7 +2095,7 @@ void launch_align_classes(const DevReads& R, RoundBuffers& B, cudaStream_t s, bo
             grid = grid_for(k_align_single, kAlignThreads, smem, 8);
         }
         // the single-warp classes share one work counter
-        k_align_single<<<grid, kAlignThreads, smem, s>>>(
+        k_align_single<<<shaped(grid, R.align_blocks), kAlignThreads, smem, s>>>(
             R, B.st, align_args(B), reinterpret_cast<int*>(B.st + 1) + kSingleWorkSlot);
         launch_align_t<2, 8, BATCH>(R, B, 4, s);
         launch_align_t<4, 8, BATCH>(R, B, 5, s);

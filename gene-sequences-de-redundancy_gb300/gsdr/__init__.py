@@ -46,6 +46,9 @@ class Opts(C.Structure):
         ("variant", C.c_int32),  # 0 cuda-version semantics, 1 the SYCL program's
         ("band_serial", C.c_int32),  # lane-banded kernel's limit; 0 automatic, -1 none
         ("group_words", C.c_int32),  # group-banded kernel's widest window; 0 automatic, -1 none
+        ("align_blocks", C.c_int32),  # block shape: CTAs per SM of the alignment kernels
+        ("filter_blocks", C.c_int32),  # the same for the word-filter kernels
+        ("graph_steps", C.c_int32),  # staging depth: rounds / passes per graph launch
     ]
 
 
@@ -85,6 +88,7 @@ class Stats(C.Structure):
         ("filter_max_bytes", C.c_double),
         ("filter_max_ms", C.c_double),
         ("cells_computed", C.c_double),
+        ("tuned", C.c_int32),
     ]
 
     def as_dict(self):
@@ -176,6 +180,8 @@ def lib():
                                               C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                               C.c_float, C.c_void_p, C.c_void_p]
         L.gsdr_set_spin_limit.argtypes = [C.c_int32, C.c_int32]
+        L.gsdr_autotune.argtypes = [P(Reads), P(Opts), C.c_int32, C.c_int32, C.c_char_p,
+                                    P(Opts), C.c_char_p, C.c_int64, P(C.c_int64)]
         L.gsdr_server_times.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
                                         C.POINTER(C.c_double)]
         L.gsdr_server_create.argtypes = [C.POINTER(ServerOpts), C.POINTER(C.c_void_p)]

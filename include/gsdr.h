@@ -66,6 +66,13 @@ typedef struct {
     int32_t group_words;  /* band tile of the group-banded alignment kernel: the widest
                              band window (32-bit words, 1..128) it takes; 0 = automatic
                              (128), -1 = none; the result is the same */
+    int32_t align_blocks; /* block shape: resident CTAs per SM the alignment kernels are
+                             launched with (1..8, capped by what fits; 0 = automatic: as
+                             many as fit); the result is the same */
+    int32_t filter_blocks; /* the same for the word-filter kernels */
+    int32_t graph_steps;  /* staging depth: rounds (plain) or passes (batched) captured in
+                             one CUDA graph, launched between two host checks of the done
+                             flag (even, 2..64; 0 = automatic: 16 plain, 4 batched) */
 } gsdr_opts;
 
 /* Reads in length-sorted order (the order readFile leaves them in).  Read i is
@@ -109,6 +116,8 @@ typedef struct {
                                  of 32 text bases, the 32-bit pattern or band-window words
                                  a warp or lane held x 32 bits x 32 bases (early exits,
                                  bands and the greedy bound make it smaller than cells) */
+    int32_t tuned;            /* 1: an automatic job (batch 0) took its knobs from the
+                                 tuning cache written by gsdr_autotune */
 } gsdr_stats;
 
 /* Fill `o` with the reference defaults (t 0.95, derived k/drop, pigeon 0). */
@@ -239,6 +248,26 @@ int gsdr_lcs_decide_noalloc(const uint32_t* d_packed, const int64_t* d_pack_off,
                             const int32_t* d_len_raw, const int32_t* d_len_gf, int32_t n_seq,
                             const int32_t* d_pat, const int32_t* d_txt, int32_t n_pairs,
                             float t, uint8_t* d_accept, void* stream);
+
+/* Autotuner: no counterpart in the reference, which has no execution knobs.
+ * Times settings of the knobs of gsdr_opts that change only the time -- R_max
+ * (batch), the batched word filter's form, the two band tiles, the block shape
+ * (align_blocks, filter_blocks) and the staging depth (graph_steps) -- by
+ * running the job on its first `reps` representatives (<= 0: min(8192,
+ * reads/20), at least 256), `runs` timed runs each (<= 0: 2), in four stages
+ * of coordinate descent; *best receives the fastest setting (the other fields
+ * as in *opts).  The result is stored in the tuning cache, one line per (GPU
+ * model and SM count, workload bucket: word length, drop mode, variant, pigeon
+ * filter, threshold, log2 of the read count and of the mean read length):
+ * at cache_path, or with cache_path NULL at $GSDR_TUNE_CACHE, else
+ * $XDG_CACHE_HOME/gsdr/tune.tsv, else $HOME/.cache/gsdr/tune.tsv; "" stores
+ * nothing.  Every later job with batch 0 in a bucket the cache holds (on the
+ * same GPU model) takes the stored knobs for each knob it leaves at 0, the
+ * `cluster` executable included (gsdr_stats.tuned = 1).  `report` (cap bytes,
+ * may be NULL) receives a JSON text of every trial; *need its size. */
+int gsdr_autotune(const gsdr_reads* reads, const gsdr_opts* opts, int32_t reps, int32_t runs,
+                  const char* cache_path, gsdr_opts* best, char* report, int64_t cap,
+                  int64_t* need);
 
 /* main (cuda-version/main.cu:3-36): the `cluster` command line.  Returns the
  * process exit status (0 also for the usage exit, as in the reference). */

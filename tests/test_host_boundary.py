@@ -165,17 +165,19 @@ def test_clstr_file_matches_format(tmp_path):
         f.close()
 
 
-def test_autotune_sample_is_whole_records():
-    from gsdr.autotune import sample_fasta
-
-    data = gsdr.synth_fasta(0, n_reads=500, seed=3)
-    s = sample_fasta(data, 100, seed=2)
-    recs = s.split(b"\n")
-    assert s.startswith(b">") and s.endswith(b"\n")
-    assert len(recs[:-1]) == 200
-    full = set(data.split(b"\n")[1::2])
-    assert all(r in full for r in recs[1:-1:2])
-    assert sample_fasta(data, 1000) == data
+@pytest.mark.parametrize("knobs,ok", [
+    (dict(align_blocks=2, filter_blocks=4, graph_steps=8), True),
+    (dict(align_blocks=9), False), (dict(filter_blocks=-1), False),
+    (dict(graph_steps=3), False), (dict(graph_steps=66), False), (dict(graph_steps=64), True),
+])
+def test_block_shape_and_staging_depth_ranges(knobs, ok):
+    o = gsdr.default_opts(**knobs)
+    if ok:
+        gsdr.resolve_opts(o)
+    else:
+        with pytest.raises(gsdr.GsdrError) as e:
+            gsdr.resolve_opts(o)
+        assert e.value.status == gsdr.EINVAL
 
 
 def test_word_filter_option_range():
@@ -271,13 +273,11 @@ def test_fasta_input_buffers():
 
 
 def test_tuned_opts_carry_every_setting():
-    from gsdr.autotune import TILES, tuned_opts
+    from gsdr.autotune import KNOBS, tuned_opts
 
-    res = {"best": {"batch": 512, "word_filter": "index", "group_words": 64,
-                    "band_serial": 4096}}
-    o = tuned_opts(res, 0.9)
-    assert (o.batch, o.word_filter, o.group_words, o.band_serial) == (512, 2, 64, 4096)
+    best = {"batch": 512, "word_filter": 2, "group_words": 64, "band_serial": 4096,
+            "align_blocks": 2, "filter_blocks": 4, "graph_steps": 8, "stage": "staging depth"}
+    o = tuned_opts({"best": best}, 0.9)
+    assert all(getattr(o, k) == best[k] for k in KNOBS)
     assert abs(o.threshold - 0.9) < 1e-6
-    # every tile the tuner tries is a valid option
-    for gw, bs in TILES:
-        gsdr.resolve_opts(gsdr.default_opts(group_words=gw, band_serial=bs))
+    gsdr.resolve_opts(o)
