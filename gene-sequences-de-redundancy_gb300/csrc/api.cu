@@ -521,7 +521,7 @@ int Job::loop_timed() {
     return rc;
 }
 
-int Job::run(int pass_limit) {
+int Job::run(int pass_limit, const int32_t* resume) {
     if (n == 0) return GSDR_OK;
     NvtxRange range_run("gsdr: job run");
     const double t0 = now_ms();
@@ -556,9 +556,17 @@ int Job::run(int pass_limit) {
     }
     JCUDA(cudaEventRecord(ev_[2], stream));
     range_prep.end();
-    // clustering / clusteringDrop (func.cu:1001-1097)
-    init_rounds(R_, B_, batched_ ? 1 : 0, r_max_, stream, pass_limit);
-    stats.kernel_launches += 1;
+    // clustering / clusteringDrop (func.cu:1001-1097), from the start or from
+    // a checkpoint's cluster array
+    if (resume) {
+        JCUDA(cudaMemcpyAsync(B_.cluster, resume, sizeof(int32_t) * n, cudaMemcpyHostToDevice,
+                              stream));
+        resume_rounds(R_, B_, batched_ ? 1 : 0, r_max_, stream, pass_limit);
+        stats.kernel_launches += 3;
+    } else {
+        init_rounds(R_, B_, batched_ ? 1 : 0, r_max_, stream, pass_limit);
+        stats.kernel_launches += 1;
+    }
     JCUDA(cudaGetLastError());
     NvtxRange range_loop(batched_ ? "gsdr: batched passes" : "gsdr: rounds");
     int rc = opts.stage_timing ? loop_timed() : loop_graph();
@@ -656,6 +664,32 @@ int gsdr_job_run(gsdr_job* j, gsdr_stats* stats) {
 int gsdr_job_run_limited(gsdr_job* j, int32_t max_passes, gsdr_stats* stats) {
     if (!j || max_passes < 1) return fail(GSDR_EINVAL, "gsdr_job_run_limited: bad argument");
     int rc = j->job.run(max_passes);
+    if (stats) *stats = j->job.stats;
+    return rc;
+}
+
+int gsdr_job_resume(gsdr_job* j, const int32_t* cluster, int32_t max_passes, gsdr_stats* stats) {
+    if (!j || (!cluster && j->job.n > 0))
+        return fail(GSDR_EINVAL, "gsdr_job_resume: null argument");
+    const int n = j->job.n;
+    // A state the greedy loop can reach: every read unclustered (-1) or joined
+    // to a representative at or before it, and every representative before the
+    // first unclustered read (representatives are taken in sorted order).
+    int first_un = n, last_rep = -1;
+    for (int i = 0; i < n; i++) {
+        const int c = cluster[i];
+        if (c == -1) {
+            if (first_un == n) first_un = i;
+            continue;
+        }
+        if (c < 0 || c > i || cluster[c] != c)
+            return fail(GSDR_EINVAL, "gsdr_job_resume: not a clustering state (cluster[i] must "
+                                     "be -1 or a representative at or before i)");
+        if (c == i) last_rep = i;
+    }
+    if (last_rep > first_un)
+        return fail(GSDR_EINVAL, "gsdr_job_resume: a representative after an unclustered read");
+    int rc = j->job.run(max_passes > 0 ? max_passes : 0, cluster);
     if (stats) *stats = j->job.stats;
     return rc;
 }

@@ -205,6 +205,11 @@ void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cud
 // device before it gives up (polls < 0: the default, kSpinLimit); for tests
 // that make a wait run out.  Returns 0 or -1 (CUDA error).
 int set_spin_limit(int polls);
+// Round state from a checkpoint instead of a fresh start: B.cluster already
+// holds the unfinished clustering (-1 = unclustered); builds the remain list,
+// the next representative (plain) or the tentative cursor (batched).
+void resume_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
+                   int pass_limit = 0);
 // One plain round (filter, align, compact, advance); `parity` picks which
 // remain buffer is the input.  `count` accumulates kernel launches; `ev4`
 // (optional) receives events around the filter and alignment stages.

@@ -26,7 +26,9 @@ public:
     // Preparation kernels + the round loop; the cluster array stays on device.
     // pass_limit > 0 stops after that many passes or rounds (timing only: the
     // clustering is then unfinished).
-    int run(int pass_limit = 0);
+    // resume (host, n entries): continue the clustering a checkpoint holds
+    // (-1 = unclustered, else the read's representative) instead of starting it
+    int run(int pass_limit = 0, const int32_t* resume = nullptr);
     // Device -> host copy of the cluster array (synchronous).
     int download(int32_t* cluster);
     // Testing: decisions of the alignment stage on given (pattern, text) pairs

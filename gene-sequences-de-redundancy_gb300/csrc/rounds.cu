@@ -945,6 +945,13 @@ __global__ void k_advance(RoundState* st, int32_t* cluster, int* align_work) {
         st->done = 1;
         return;
     }
+    // a run stopped after pass_limit rounds (timing runs, checkpoints) leaves
+    // the next representative unclustered, so that cluster[] alone is the
+    // loop's state: a resumed run takes it as the smallest unclustered read
+    if (st->pass_limit > 0 && st->passes >= st->pass_limit) {
+        st->done = 1;
+        return;
+    }
     const int rep = st->next_min;
     cluster[rep] = rep;
     st->rep = rep;
@@ -952,7 +959,6 @@ __global__ void k_advance(RoundState* st, int32_t* cluster, int* align_work) {
     st->n_next = 0;
     st->next_min = 0x7fffffff;
     reset_align_counters(st, align_work);
-    if (st->pass_limit > 0 && st->passes >= st->pass_limit) st->done = 1;  // timing runs
 }
 
 // ---------------------------------------------------------------- batched form
@@ -1845,6 +1851,67 @@ __global__ void k_init(RoundState* st, int32_t* cluster, int32_t* remain, uint32
     }
 }
 
+// Resume from a checkpoint: cluster[] (already on the device) is the state of
+// an unfinished clustering -- every read either unclustered (-1) or joined to
+// a representative taken earlier -- which is all the state the reference's
+// loop carries between rounds (cluster[] and the next representative, the
+// smallest unclustered read; cuda-version/func.cu:1001-1066).  Three steps:
+// a fresh round state, the remain list of the unclustered reads (any order:
+// every consumer of the list is order-independent) with their smallest index,
+// then the next representative (plain) or the tentative cursor (batched).
+__global__ void k_resume_state(RoundState* st, int r_max, int pass_limit, int* align_work) {
+    RoundState s = {};
+    s.rep = -1;
+    s.next_min = 0x7fffffff;
+    s.pass = 1;
+    s.R = 1;
+    s.R_max = r_max;
+    s.pass_limit = pass_limit;
+    *st = s;
+    for (int c = 0; c <= kSingleWorkSlot; c++) align_work[c] = 0;
+}
+
+__global__ void k_resume_scan(RoundState* st, const int32_t* __restrict__ cluster,
+                              int32_t* remain, uint32_t* tidx, uint32_t* best, int n,
+                              int batched) {
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int i = base + lane;
+        const bool un = i < n && cluster[i] == -1;
+        if (batched && i < n) {
+            tidx[i] = 0xffffffffu;
+            best[i] = 0u;
+        }
+        const unsigned m = __ballot_sync(kFull, un);
+        if (!m) continue;
+        int pos = 0;
+        if (lane == 0) {
+            pos = atomicAdd(&st->n_remain, __popc(m));
+            atomicMin(&st->next_min, base + __ffs(m) - 1);
+        }
+        pos = __shfl_sync(kFull, pos, 0);
+        if (un) remain[pos + __popc(m & ((1u << lane) - 1u))] = i;
+    }
+}
+
+__global__ void k_resume_start(RoundState* st, int32_t* cluster, int batched) {
+    if (st->n_remain == 0) {
+        st->done = 1;
+        return;
+    }
+    const int first = st->next_min;
+    st->next_min = 0x7fffffff;
+    if (batched) {
+        st->cursor = first;
+    } else {
+        // the next round's representative; it stays in the remain list, which
+        // the plain filter skips, as after every compaction
+        cluster[first] = first;
+        st->rep = first;
+    }
+}
+
 // ---------------------------------------------------------------- launchers
 
 template <class KernelT>
@@ -2123,6 +2190,17 @@ void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cud
     const int blocks = n > 0 ? (n + threads - 1) / threads : 1;
     k_init<<<blocks, threads, 0, s>>>(B.st, B.cluster, B.remain[0], B.tidx, B.best, n, batched,
                                       r_max, pass_limit, align_work_of(B.st));
+}
+
+void resume_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
+                   int pass_limit) {
+    const int n = R.n;
+    k_resume_state<<<1, 1, 0, s>>>(B.st, r_max, pass_limit, align_work_of(B.st));
+    const int want = (n + 255) / 256, cap = num_sms() * 8;
+    const int blocks = n > 0 ? (want < cap ? want : cap) : 1;
+    k_resume_scan<<<blocks, 256, 0, s>>>(B.st, B.cluster, B.remain[0], B.tidx, B.best, n,
+                                         batched);
+    k_resume_start<<<1, 1, 0, s>>>(B.st, B.cluster, batched);
 }
 
 void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,

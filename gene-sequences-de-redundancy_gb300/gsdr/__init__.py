@@ -180,6 +180,7 @@ def lib():
                                               C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                               C.c_float, C.c_void_p, C.c_void_p]
         L.gsdr_set_spin_limit.argtypes = [C.c_int32, C.c_int32]
+        L.gsdr_job_resume.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, P(Stats)]
         L.gsdr_autotune.argtypes = [P(Reads), P(Opts), C.c_int32, C.c_int32, C.c_char_p,
                                     P(Opts), C.c_char_p, C.c_int64, P(C.c_int64)]
         L.gsdr_server_times.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
@@ -401,13 +402,25 @@ class Job:
         self._h = h
 
     def run(self, max_passes: int = 0) -> Stats:
-        """gsdr_job_run; with max_passes > 0, gsdr_job_run_limited (timing only:
-        the clustering stops unfinished after that many passes)."""
+        """gsdr_job_run; with max_passes > 0, gsdr_job_run_limited (the
+        clustering stops unfinished after that many passes or rounds; its
+        cluster() is then a checkpoint for resume)."""
         st = Stats()
         if max_passes > 0:
             _check(lib().gsdr_job_run_limited(self._h, max_passes, C.byref(st)))
         else:
             _check(lib().gsdr_job_run(self._h, C.byref(st)))
+        return st
+
+    def resume(self, checkpoint: np.ndarray, max_passes: int = 0) -> Stats:
+        """gsdr_job_resume: continues the unfinished clustering `checkpoint`
+        (a cluster array, -1 = unclustered) for max_passes more passes or
+        rounds (0: to the end)."""
+        cp = np.ascontiguousarray(checkpoint, dtype=np.int32)
+        if len(cp) != self.n:
+            raise GsdrError(EINVAL, "checkpoint size differs from the job's read count")
+        st = Stats()
+        _check(lib().gsdr_job_resume(self._h, cp.ctypes.data, max_passes, C.byref(st)))
         return st
 
     def cluster(self) -> np.ndarray:

@@ -212,6 +212,21 @@ int gsdr_job_run(gsdr_job* job, gsdr_stats* stats);
 int gsdr_job_cluster(gsdr_job* job, int32_t* cluster);
 void gsdr_job_free(gsdr_job* job);
 
+/* Checkpoint / resume.  The whole state the reference's round loop carries
+ * from one round to the next is cluster[] (func.cu:1001-1066): the next
+ * representative is the smallest unclustered read.  So a checkpoint is the
+ * cluster array of an unfinished run -- gsdr_job_cluster after a run stopped
+ * early (gsdr_job_run_limited, include/gsdr_testing.h), -1 for unclustered
+ * reads -- which the caller may save anywhere.  gsdr_job_resume continues
+ * that clustering on a job over the same reads and options (the same or
+ * another job, in this or another process) for up to max_passes more passes
+ * or rounds (<= 0: to the end); the finished result equals an uninterrupted
+ * run's.  GSDR_EINVAL unless every cluster[i] is -1 or a representative
+ * c <= i with cluster[c] == c, and no representative comes after an
+ * unclustered read. */
+int gsdr_job_resume(gsdr_job* job, const int32_t* cluster, int32_t max_passes,
+                    gsdr_stats* stats);
+
 /* The alignment-stage decision for callers that cannot allocate device memory.
  * No counterpart in the reference.  Some callers own every device allocation:
  * code inside a framework's memory pool or a plug-in that must not grow the
