@@ -340,7 +340,7 @@ def serve_stream(jobs, gaps, device, max_inflight):
                 srv.release(jid)
     finally:
         srv.close()
-    rows = [(status.get(j), lat.get(j), run.get(j), n) for j, n in ids]
+    rows = [(status.get(j), lat.get(j), run.get(j), n, jobs[k][1]) for k, (j, n) in enumerate(ids)]
     return rows, wall, results
 
 
@@ -381,8 +381,20 @@ def serving_run(args, device):
                 match = match and len(ocl) == len(cl) and bool((ocl == cl).all())
     except Exception as e:  # the checker is optional here; say why it did not run
         match = f"not checked: {e}"
+    by_t = {}
+    for r in ok:
+        b = by_t.setdefault(f"{r[4]:.2f}", {"jobs": 0, "reads": 0, "run_ms": 0.0,
+                                             "max_run_ms": 0.0, "latency_ms": 0.0})
+        b["jobs"] += 1
+        b["reads"] += r[3]
+        b["run_ms"] += r[2] or 0.0
+        b["max_run_ms"] = max(b["max_run_ms"], r[2] or 0.0)
+        b["latency_ms"] += r[1]
+    for b in by_t.values():
+        b["mean_run_ms"] = b.pop("run_ms") / b["jobs"]
+        b["mean_latency_ms"] = b.pop("latency_ms") / b["jobs"]
     return {
-        "jobs": len(rows), "completed": len(ok),
+        "jobs": len(rows), "completed": len(ok), "by_threshold": by_t,
         "rejected_t1": sum(1 for r in rows if r[0] == 1),
         "failed": sum(1 for r in rows if r[0] not in (0, 1)),
         "arrival_rate_per_s": args.serving_rate,
