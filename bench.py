@@ -360,8 +360,9 @@ def serving_run(args, device):
     ls = np.array([r[1] for r in ok]) if ok else np.array([0.0])
     busy = sum(r[2] for r in ok if r[2] is not None) / 1e3
     done_reads = sum(r[3] for r in ok)
-    # overlap: 32 filter-mode jobs of the stream, all submitted at once
-    burst = [j for j in jobs if j[1] >= 0.88 and j[1] < 1.0][:32]
+    # overlap: 32 filter-mode jobs of the stream of at most 20k reads (jobs too
+    # small to fill the device alone), all submitted at once
+    burst = [j for j in jobs if 0.88 <= j[1] < 1.0 and j[2] <= 20000][:32]
     _, wall1, _ = serve_stream(burst, None, device, 1)
     _, wall4, _ = serve_stream(burst, None, device, 4)
     # a sample of served results against the oracle

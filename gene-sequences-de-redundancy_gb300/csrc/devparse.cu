@@ -368,8 +368,23 @@ struct DevBuf {
 
 }  // namespace
 
+gsdr_result* new_result() { return new (std::nothrow) gsdr_result(); }
+
+int64_t cluster_fasta_parse_bytes(int64_t n, int64_t records, int64_t newlines) {
+    const int64_t n_chunks = (n + kChunk - 1) / kChunk + 1;
+    const int64_t lines = newlines + 2;
+    return (2 * n + 64)                                  // the file, concatenated records
+           + 4 * (n / (kScanThreads * kScanItems) + 8) + 64 + 4 * n_chunks  // scans, counts
+           + 8 * lines                                   // newline positions
+           + 8 * lines                                   // line kinds
+           + 40 * (records + 1)                          // record heads, names, data spans
+           + 12 * (records + 1) + 48                     // output order, sizes, offsets
+           + n + 16                                      // output records (at most the file)
+           + (1 << 20);                                  // allocation rounding
+}
+
 int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_result* res,
-                  gsdr_stats* stats) {
+                  gsdr_stats* stats, const std::function<int(int64_t)>* admit) {
     gsdr_opts o = *opts_in;
     int rc = gsdr_resolve_opts(&o, nullptr);
     if (rc) return rc;
@@ -529,6 +544,13 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     gsdr_reads view{reinterpret_cast<const char*>(b), n + 16 + extra, s_off.data(),
                     res->length.data(), nr};
     res->cluster.assign(nr > 0 ? nr : 1, 0);
+    if (admit) {
+        // the serving loop's admission by device footprint: it may block here
+        const int64_t need = Job::footprint(&view, &o);
+        if (need < 0) return fail(GSDR_EINVAL, "cluster_fasta: cannot size the job");
+        rc = (*admit)(need);
+        if (rc) return rc;
+    }
     Job job;
     rc = job.init(&view, &o, s);
     mark("job_init");

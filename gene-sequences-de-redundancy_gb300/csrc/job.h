@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <vector>
 
 #include "gsdr.h"
@@ -71,6 +72,21 @@ private:
     DevReads R_{};
     RoundBuffers B_{};
 };
+
+// devparse.cu: gsdr_cluster_fasta's path (device parse, host sort, clustering,
+// device formatting) on its own stream.  admit (may be null) is called with
+// the job's device footprint once the reads are known and before the job's
+// memory is taken; a non-zero return ends the call with that status (the
+// serving loop blocks there until the job fits its memory budget).
+int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts, gsdr_result* res,
+                  gsdr_stats* stats, const std::function<int(int64_t)>* admit = nullptr);
+// An empty result for cluster_fasta (nullptr without host memory); released
+// with gsdr_result_free.
+gsdr_result* new_result();
+// Device bytes gsdr_cluster_fasta takes beside the job's own for a file of n
+// bytes with at most `records` records and `newlines` newlines (the file
+// twice, the line and record arrays, the output records): an upper bound.
+int64_t cluster_fasta_parse_bytes(int64_t n, int64_t records, int64_t newlines);
 
 // autotune.cu: the tuning cache's knobs for this workload's bucket on this
 // GPU, applied to every knob `o` leaves automatic (only when o.batch == 0);

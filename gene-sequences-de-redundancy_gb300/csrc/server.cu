@@ -1,20 +1,34 @@
 // server.cu -- serving: continuous batching of independent clustering jobs on
 // one GPU (gsdr_server_* in include/gsdr.h; no counterpart in the reference).
 //
-// Jobs arrive as FASTA bytes with their own threshold.  A scheduler thread
-// takes them in arrival order, parses each one (the reference's readFile rules
-// and sort), computes its device footprint and admits it as soon as a slot is
-// free (max_inflight) and its footprint fits the remaining memory budget.  An
-// admitted job runs on its own worker thread and CUDA stream through the same
-// gsdr::Job as gsdr_cluster, so jobs overlap on the device and each result is
-// exactly what gsdr_cluster returns for that job alone.  A job larger than the
-// whole budget waits until nothing else runs and then runs alone.
+// Jobs arrive as FASTA bytes with their own threshold.  Each job runs the
+// gsdr_cluster_fasta path on a worker thread and its own CUDA stream: the
+// file goes to the device once, records are found there, the lengths come
+// back for the reference's std::sort, the job clusters the device-resident
+// reads and the representative records are formatted on the device.  So jobs
+// overlap on the device, the host work of one job (its sort) overlaps the
+// device work of the others, and each result is exactly what
+// gsdr_cluster_fasta returns for that job alone.
+//
+// Admission by device footprint, in two steps against the memory budget:
+//   1. the scheduler thread admits a job to a free slot (max_inflight) when
+//      an upper bound of its parse buffers (from its byte, record and newline
+//      counts, taken at submission) fits the remaining budget;
+//   2. once the worker knows the reads, the job's exact clustering footprint
+//      must fit too; the worker waits for it while the job's parse buffers
+//      are held.
+// A job that does not fit waits until no other job is clustering and then
+// runs alone, so every job is served.  Device memory comes from the library's
+// stream-ordered pool (devmem.h): a finished job's release waits for nothing
+// but its own stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -32,17 +46,16 @@ namespace gsdr {
 struct ServerJob {
     int64_t id = 0;
     std::vector<char> fasta;
+    int64_t records = 0, newlines = 0;  // upper bounds, counted at submission
     float threshold = 0.95f;
     double t_submit = 0, t_start = 0, t_done = 0;
     int status = GSDR_OK;
     std::string error;
-    gsdr_fasta* parsed = nullptr;
     std::vector<int32_t> cluster;
     std::vector<char> out;
-    int64_t footprint = 0;
-    ~ServerJob() {
-        if (parsed) gsdr_fasta_free(parsed);
-    }
+    int64_t parse_bytes = 0;  // step-1 reservation
+    int64_t job_bytes = 0;    // step-2 reservation
+    bool clustering = false;
 };
 
 }  // namespace gsdr
@@ -63,12 +76,20 @@ struct gsdr_server {
     std::thread scheduler;
     bool workers_stop = false;
     int inflight = 0;
+    int clustering = 0;                // jobs past step 2
     int64_t mem_used = 0;
     int64_t next_id = 1;
     bool stopping = false;
 };
 
 namespace {
+
+void finish(gsdr_server* s, const std::shared_ptr<ServerJob>& j, int rc) {
+    j->status = rc;
+    j->t_done = now_ms();
+    s->finished.push_back(j->id);
+    s->cv_done.notify_all();
+}
 
 void run_job(gsdr_server* s, std::shared_ptr<ServerJob> j) {
     j->t_start = now_ms();
@@ -77,32 +98,43 @@ void run_job(gsdr_server* s, std::shared_ptr<ServerJob> j) {
     o.threshold = j->threshold;
     o.device = s->so.device;
     o.batch = s->so.batch;
-    gsdr_reads v;
-    gsdr_fasta_view(j->parsed, &v);
-    j->cluster.assign(v.n > 0 ? v.n : 1, 0);
+    // step 2 of the admission: the job's own footprint, once its reads are known
+    const std::function<int(int64_t)> admit = [s, j](int64_t need) -> int {
+        std::unique_lock<std::mutex> lock(s->mu);
+        s->cv_sched.wait(lock, [&] {
+            return s->stopping || s->mem_used + need <= s->so.mem_budget || s->clustering == 0;
+        });
+        if (s->stopping) return fail(GSDR_EBUSY, "server stopped");
+        s->mem_used += need;
+        j->job_bytes = need;
+        j->clustering = true;
+        s->clustering++;
+        return GSDR_OK;
+    };
     int rc = GSDR_OK;
-    {
-        Job job;
-        rc = job.init(&v, &o);
-        if (!rc) rc = job.upload(&v);
-        if (!rc) rc = job.run();
-        if (!rc) rc = job.download(j->cluster.data());
-        if (rc) j->error = gsdr_last_error();
-    }
+    std::unique_ptr<gsdr_result, void (*)(gsdr_result*)> r(new_result(), gsdr_result_free);
+    if (!r) rc = fail(GSDR_ENOMEM, "server: out of host memory");
+    if (!rc)
+        rc = cluster_fasta(j->fasta.data(), (int64_t)j->fasta.size(), &o, r.get(), nullptr,
+                           &admit);
     if (!rc) {
-        int64_t need = 0;
-        gsdr_fasta_format(j->parsed, j->cluster.data(), nullptr, 0, &need);
-        j->out.resize((size_t)need);
-        rc = gsdr_fasta_format(j->parsed, j->cluster.data(), j->out.data(), need, &need);
+        const char* data = nullptr;
+        int64_t nb = 0;
+        gsdr_result_output(r.get(), &data, &nb);
+        j->out.assign(data, data + nb);
+        const int32_t* cl = gsdr_result_cluster(r.get());
+        j->cluster.assign(cl, cl + gsdr_result_count(r.get()));
+    } else {
+        j->error = gsdr_last_error();
     }
-    j->cluster.resize(v.n > 0 ? v.n : 0);
+    r.reset();
+    j->fasta.clear();
+    j->fasta.shrink_to_fit();
     std::lock_guard<std::mutex> lock(s->mu);
-    j->status = rc;
-    j->t_done = now_ms();
     s->inflight--;
-    s->mem_used -= j->footprint;
-    s->finished.push_back(j->id);
-    s->cv_done.notify_all();
+    s->mem_used -= j->parse_bytes + j->job_bytes;
+    if (j->clustering) s->clustering--;
+    finish(s, j, rc);
     s->cv_sched.notify_all();
 }
 
@@ -117,46 +149,32 @@ void scheduler_loop(gsdr_server* s) {
             j = s->queue.front();
             s->queue.pop_front();
         }
-        // parse and size the job outside the lock
         gsdr_opts o;
         gsdr_default_opts(&o);
         o.threshold = j->threshold;
         o.batch = s->so.batch;
-        int rc = gsdr_resolve_opts(&o, nullptr);
-        if (!rc) rc = gsdr_fasta_parse(j->fasta.data(), (int64_t)j->fasta.size(), &j->parsed);
-        if (!rc) {
-            gsdr_reads v;
-            gsdr_fasta_view(j->parsed, &v);
-            j->footprint = Job::footprint(&v, &o);
-            if (j->footprint < 0) rc = GSDR_EINVAL;
-        }
-        j->fasta.clear();
-        j->fasta.shrink_to_fit();
+        const int rc = gsdr_resolve_opts(&o, nullptr);
         std::unique_lock<std::mutex> lock(s->mu);
-        if (rc) {
-            j->status = rc;
+        if (rc) {  // t outside [0.8, 1): refused as checkOption refuses it
             j->error = gsdr_last_error();
-            j->t_done = now_ms();
-            s->finished.push_back(j->id);
-            s->cv_done.notify_all();
+            finish(s, j, rc);
             continue;
         }
-        // admission: a free slot and room in the budget (or nothing running)
+        j->parse_bytes = cluster_fasta_parse_bytes((int64_t)j->fasta.size(), j->records,
+                                                   j->newlines);
+        // step 1: a free slot and room for the parse buffers (or nothing running)
         s->cv_sched.wait(lock, [&] {
             return s->stopping || (s->inflight < s->so.max_inflight &&
-                                   (s->mem_used + j->footprint <= s->so.mem_budget ||
+                                   (s->mem_used + j->parse_bytes <= s->so.mem_budget ||
                                     s->inflight == 0));
         });
         if (s->stopping) {
-            j->status = GSDR_EBUSY;
             j->error = "server stopped";
-            j->t_done = now_ms();
-            s->finished.push_back(j->id);
-            s->cv_done.notify_all();
+            finish(s, j, GSDR_EBUSY);
             continue;
         }
         s->inflight++;
-        s->mem_used += j->footprint;
+        s->mem_used += j->parse_bytes;
         s->ready.push_back(j);
         s->cv_work.notify_one();
     }
@@ -216,6 +234,10 @@ int gsdr_server_submit(gsdr_server* s, const char* fasta, int64_t n, float thres
     } catch (const std::bad_alloc&) {
         return fail(GSDR_ENOMEM, "server: out of host memory");
     }
+    // bounds for the parse buffers: every '>' may open a record (and the first
+    // line always does), every newline ends a line
+    j->records = (int64_t)std::count(j->fasta.begin(), j->fasta.end(), '>') + 1;
+    j->newlines = (int64_t)std::count(j->fasta.begin(), j->fasta.end(), '\n');
     j->threshold = threshold;
     j->t_submit = now_ms();
     std::lock_guard<std::mutex> lock(s->mu);
