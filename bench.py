@@ -191,8 +191,27 @@ def filter_roofline(r, figures):
             "stage_ms": r["filter_ms"],
             "heaviest_launch": heaviest_launch(r["filter_max_bytes"], r["filter_max_ms"],
                                                r["peak"]),
-            "note": "batched: R tentatives are tested per streamed byte, so the stage is "
-                    "bound by shared-memory lookups / popcounts, not by HBM"}
+            "measured_bound": measured_filter_bound(form, figures),
+            "note": "R tentatives per streamed byte: the measured bound is on chip "
+                    "(measured_bound, ncu), not HBM"}
+
+
+def measured_filter_bound(form, figures):
+    """The filter kernel's binding resource as ncu measured it (profiles/)."""
+    if form == "table" and figures.get("c1.filter_table.l1tex_pct") is not None:
+        return {"resource": "L1TEX / shared memory", "kernel": "k_bfilter_tab<6>",
+                "l1tex_pct_of_peak": figures["c1.filter_table.l1tex_pct"],
+                "smem_roofline_frac": figures.get(
+                    "c1.filter_table.smem_wavefronts_per_sm_cycle"),
+                "bank_conflict_wavefront_share": figures.get(
+                    "c1.filter_table.bank_conflict_wavefront_share"),
+                "source": "profiles/k_bfilter_tab_c1_smem.md (200k-read workload)"}
+    if form == "index" and figures.get("c2.filter_index.ipc") is not None:
+        return {"resource": "instruction issue", "kernel": "k_bfilter_idx<7>",
+                "ipc_of_4": figures["c2.filter_index.ipc"],
+                "alu_pipe_pct": figures.get("c2.filter_index.alu_pipe_pct"),
+                "source": "profiles/k_bfilter_idx_c2_300k.md (2M-read workload slice)"}
+    return None
 
 
 def align_roofline(r, figures):
