@@ -148,10 +148,10 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
         if (form == 2) index = true, bits = false;
         if (form == 3) index = false, bits = k <= kMaxBitsK;
         P.bits = bits;
-        // automatic R with the table form: the largest R (measured fastest on
-        // the 200k-read workload by gsdr/autotune.py: 22.6 us per
-        // representative at R_max 1024 against 25.5 at 256)
-        if (o.batch == 0 && !index && !bits) P.r_max = kMaxBatch;
+        // automatic R with the table and bitmap forms: the largest R (the
+        // table form measured fastest at R_max 1024 on the 200k-read
+        // workload: 22.6 us per representative against 25.5 at 256)
+        if (o.batch == 0 && !index) P.r_max = kMaxBatch;
         if (index) {
             // a pass indexes at most R_max tentatives: for length-sorted reads
             // those hold at most the first R_max reads' entries
@@ -201,6 +201,8 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     const size_t nbw = bits ? ((size_t)1 << (2 * k)) / 32 : 0;
     R.kbits = bits ? c.take<uint32_t>((size_t)n * nbw) : nullptr;
     R.kextra = bits ? c.take<int32_t>(n) : nullptr;
+    R.kbits2 = P.bits ? c.take<uint32_t>((size_t)n * nbw) : nullptr;
+    R.kextra3 = P.bits ? c.take<int32_t>(n) : nullptr;
     B.st = reinterpret_cast<RoundState*>(c.take<char>(sizeof(RoundState) + 4 * 64));
     B.cluster = c.take<int32_t>(n);
     B.remain[0] = c.take<int32_t>(n);

@@ -69,6 +69,12 @@ struct DevReads {
     // multiplicity excess sum(count) - #distinct over those k-mers
     uint32_t* kbits;
     int32_t* kextra;
+    // batched bitmap filter only (null otherwise): the second count level --
+    // bitmap of the k-mers with a stored multiplicity of 2 or more (same
+    // layout as kbits) and the excess above two, sum over k-mers of
+    // max(count - 2, 0)
+    uint32_t* kbits2;
+    int32_t* kextra3;
     // pigeon filter (p 1; null otherwise), the reference's 4-mer position
     // index: pig[256 i + v] = inclusive prefix of read i's 4-mer bucket counts
     // (u16), pidx[off[i] + slot] = (u16) absolute position of a window's last

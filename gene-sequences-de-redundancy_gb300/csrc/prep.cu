@@ -194,13 +194,15 @@ __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
     extern __shared__ __align__(16) uint32_t sm[];
     uint32_t* hist = sm;
     uint16_t* list = reinterpret_cast<uint16_t*>(sm + NB);
-    __shared__ uint32_t bits[NBW];
-    __shared__ int nlist, sumcnt;
+    __shared__ uint32_t bits[NBW], bits2[NBW];
+    __shared__ int nlist, sumcnt, sum3;
+    const bool level2 = BITS && R.kbits2 != nullptr;
     for (int i = threadIdx.x; i < NB; i += blockDim.x) hist[i] = 0;
-    for (int i = threadIdx.x; i < NBW; i += blockDim.x) bits[i] = 0;
+    for (int i = threadIdx.x; i < NBW; i += blockDim.x) bits[i] = bits2[i] = 0;
     if (threadIdx.x == 0) {
         nlist = 0;
         sumcnt = 0;
+        sum3 = 0;
     }
     __syncthreads();
     for (int r = blockIdx.x; r < R.n; r += gridDim.x) {
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
         }
         __syncthreads();
         const int nl = nlist;
-        int my_sum = 0;
+        int my_sum = 0, my_sum3 = 0;
         for (int s = threadIdx.x; s < nl; s += blockDim.x) {
             const uint32_t km = list[s];
             const uint32_t c = hist[km] & 0xffffu;  // the reference's u16 multiplicity
@@ -228,6 +230,10 @@ __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
             if (BITS && c) {
                 atomicOr(&bits[km >> 5], 1u << (km & 31));
                 my_sum += (int)c - 1;
+                if (level2 && c >= 2) {
+                    atomicOr(&bits2[km >> 5], 1u << (km & 31));
+                    my_sum3 += (int)c - 2;
+                }
             }
         }
         const int padded = (nl + 3) & ~3;
@@ -235,6 +241,10 @@ __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
         if (BITS) {
             my_sum = warp_sum(my_sum);
             if ((threadIdx.x & 31) == 0 && my_sum) atomicAdd(&sumcnt, my_sum);
+            if (level2) {
+                my_sum3 = warp_sum(my_sum3);
+                if ((threadIdx.x & 31) == 0 && my_sum3) atomicAdd(&sum3, my_sum3);
+            }
         }
         __syncthreads();
         if (BITS) {
@@ -243,12 +253,21 @@ __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
                 ob[i] = bits[i];
                 bits[i] = 0;
             }
+            if (level2) {
+                uint32_t* ob2 = R.kbits2 + (size_t)r * NBW;
+                for (int i = threadIdx.x; i < NBW; i += blockDim.x) {
+                    ob2[i] = bits2[i];
+                    bits2[i] = 0;
+                }
+            }
         }
         if (threadIdx.x == 0) {
             R.n_kmer[r] = nl;
             if (BITS) R.kextra[r] = sumcnt;
+            if (level2) R.kextra3[r] = sum3;
             nlist = 0;
             sumcnt = 0;
+            sum3 = 0;
         }
         __syncthreads();
     }

@@ -1219,39 +1219,62 @@ __global__ void __launch_bounds__(kFilterThreads) k_bprefilter(DevReads R, Round
     }
 }
 
-// ---- word filter by k-mer presence bitmaps (k <= kMaxBitsK) ----------------
+// ---- word filter by two-level k-mer count bitmaps (k <= kMaxBitsK) --------
 //
-// With D = the number of k-mers both reads hold (non-zero stored counts) and
-// E = a read's count excess (sum of counts minus distinct k-mers), the word
-// sum S of kernel_filter (func.cu:803-826) satisfies D <= S <= D + min(E_t,
-// E_q): every shared k-mer adds at least one and at most one plus its excess.
-// D is a popcount over the two 4^k-bit bitmaps, so k_bfilter_bits decides
-// almost every pair with 4^k / 32 AND + POPC per lane instead of one table
-// lookup per k-mer; the few pairs the bound leaves open go to k_bexact, which
-// forms S itself.
+// Per read two 4^k-bit bitmaps: level 1 holds the k-mers with a stored count
+// of at least one, level 2 those with at least two; E3 is the excess above
+// two, sum over k-mers of max(count - 2, 0).  The word sum of kernel_filter
+// (func.cu:803-826) is S = sum over k-mers of min(c_t, c_q), and since
+// min(c_t, c_q) = [both >= 1] + [both >= 2] + max(min(c_t, c_q) - 2, 0),
+//     lo = D1 + D2 <= S <= lo + min(E3_t, E3_q),
+// with D1, D2 the popcounts of the two levels' intersections.  k_bfilter_bits
+// forms lo with 2 x 4^k / 32 AND + POPC per pair (lane = tentative, no table
+// lookups, no bank conflicts) and decides every pair outside the gap; the few
+// pairs inside it go to k_bexact, which forms S itself.  The second level
+// keeps the gap small where one level leaves it wide (reads holding a large
+// share of the k-mer space, whose counts are mostly 1 or 2).
 
-constexpr int kBitsGroup = 64;  // tentatives staged per CTA
+constexpr int kBitsGroup = 128;    // tentatives staged per CTA
+constexpr int kBitsThreads = 1024;
+
+// Shared memory of k_bfilter_bits: the group's two bitmap levels as
+// [level][quad][tentative] (lane t reads consecutive 16 bytes: conflict-free),
+// each warp's candidate bitmaps, and the group's tentatives, compositions and
+// excesses.
+template <int K>
+struct BitsSmem {
+    static constexpr int NQ = (1 << (2 * K)) / 128;  // 16-byte words of one bitmap
+    static constexpr int WARPS = kBitsThreads / 32;
+    static constexpr size_t tb_quads = 2 * (size_t)NQ * kBitsGroup;
+    static constexpr size_t cb_quads = (size_t)WARPS * 2 * NQ;
+    static constexpr size_t bytes = 16 * (tb_quads + cb_quads) + kBitsGroup * (16 + 4 + 4);
+};
 
 template <int K>
-__global__ void __launch_bounds__(kFilterThreads) k_bfilter_bits(DevReads R, RoundState* st,
-                                                                 const int32_t* __restrict__ remain,
-                                                                 const int32_t* __restrict__ tent,
-                                                                 Pair* pairs, int seg_cap, Pair* amb) {
-    constexpr int NQ = (1 << (2 * K)) / 128;  // 16-byte words of a bitmap
+__global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, RoundState* st,
+                                                                  const int32_t* __restrict__ remain,
+                                                                  const int32_t* __restrict__ tent,
+                                                                  Pair* pairs, int seg_cap, Pair* amb) {
+    using L = BitsSmem<K>;
+    constexpr int NQ = L::NQ;
     constexpr int RG = kBitsGroup;
-    constexpr int WARPS = kFilterThreads / 32;
-    // tentative bitmaps as [quad][tentative]: lane t reads consecutive 16 bytes
-    __shared__ __align__(16) uint4 tb[NQ][RG];
-    __shared__ __align__(16) uint4 cb[WARPS][NQ];
-    __shared__ int4 tcomp[RG];
-    __shared__ int ttent[RG], textra[RG];
-    if (st->done || st->n_tent == 0) return;
+    constexpr int WARPS = L::WARPS;
+    extern __shared__ __align__(16) uint4 bsm[];
+    uint4* tb = bsm;                                  // tb[(level * NQ + w) * RG + t]
+    uint4* cball = bsm + L::tb_quads;                 // cb[(warp * 2 + level) * NQ + w]
+    int4* tcomp = reinterpret_cast<int4*>(cball + L::cb_quads);
+    int* ttent = reinterpret_cast<int*>(tcomp + RG);
+    int* textra = ttent + RG;
+    if (st->done) return;
     const int nt = st->n_tent;
+    if (nt <= 1) return;  // a single tentative's pass runs k_filter instead
     const int n = st->n_remain;
     const int ngroups = (nt + RG - 1) / RG;
     const int parts = max(1, (int)gridDim.x / ngroups);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint4* kb4 = reinterpret_cast<const uint4*>(R.kbits);
+    uint4* cb = cball + warp * 2 * NQ;
+    const uint4* kb1 = reinterpret_cast<const uint4*>(R.kbits);
+    const uint4* kb2 = reinterpret_cast<const uint4*>(R.kbits2);
     unsigned n_pf = 0, n_wf = 0, n_al = 0;
     unsigned long long bytes = 0;
     int cur_group = -1;
@@ -1262,16 +1285,17 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter_bits(DevReads R, Rou
         if (g != cur_group) {
             __syncthreads();
             if (threadIdx.x < RG) {
-                const int i = t0 + threadIdx.x;
-                const bool in = threadIdx.x < ng;
-                const int rep = in ? tent[i] : 0;
+                const bool in = (int)threadIdx.x < ng;
+                const int rep = in ? tent[t0 + threadIdx.x] : 0;
                 ttent[threadIdx.x] = in ? rep : 0x7fffffff;
                 tcomp[threadIdx.x] = in ? R.comp[rep] : make_int4(0, 0, 0, 0);
-                textra[threadIdx.x] = in ? R.kextra[rep] : 0;
+                textra[threadIdx.x] = in ? R.kextra3[rep] : 0;
             }
-            for (int i = threadIdx.x; i < ng * NQ; i += kFilterThreads) {
-                const int t = i / NQ, w = i % NQ;
-                tb[w][t] = __ldg(kb4 + (size_t)tent[t0 + t] * NQ + w);
+            for (int i = threadIdx.x; i < 2 * NQ * RG; i += kBitsThreads) {
+                const int t = i % RG, lw = i / RG, lv = lw / NQ, w = lw % NQ;
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (t < ng) v = __ldg((lv ? kb2 : kb1) + (size_t)tent[t0 + t] * NQ + w);
+                tb[i] = v;
             }
             __syncthreads();
             cur_group = g;
@@ -1280,7 +1304,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter_bits(DevReads R, Rou
         const int lo = part * per, hi = min(n, lo + per);
         for (int idx = lo + warp; idx < hi; idx += WARPS) {
             const int q = remain[idx];
-            if (g == 0) bytes += kCandFixedBytes + 16ull * NQ;  // once per launch
+            if (g == 0) bytes += kCandFixedBytes + 2ull * 16 * NQ;  // once per launch
             const int4 cq = R.comp[q];
             const int cbq = R.cut_base[q] - R.strict;  // the prefilter's cutoff
             unsigned ok_bits[RG / 32];
@@ -1290,26 +1314,30 @@ __global__ void __launch_bounds__(kFilterThreads) k_bfilter_bits(DevReads R, Rou
                 const int t = 32 * h + lane;
                 const bool before = t < ng && ttent[t] < q;
                 n_pf += before;
+                // kernel_preFilter (func.cu:738-754) first
                 const bool ok = before && prefilter_pass(tcomp[t], cq, cbq);
                 ok_bits[h] = __ballot_sync(kFull, ok);
                 any |= ok_bits[h] != 0;
             }
             if (!any) continue;
-            for (int i = lane; i < NQ; i += 32) cb[warp][i] = __ldcs(kb4 + (size_t)q * NQ + i);
+            for (int i = lane; i < 2 * NQ; i += 32)
+                cb[i] = __ldcs((i < NQ ? kb1 : kb2) + (size_t)q * NQ + (i % NQ));
             __syncwarp();
             const int cw = R.cut_word[q];
-            const int exq = R.kextra[q];
+            const int exq = R.kextra3[q];
 #pragma unroll
             for (int h = 0; h < RG / 32; h++) {
                 if (!ok_bits[h]) continue;
                 const int t = 32 * h + lane;
                 int d = 0;
-#pragma unroll 8
+#pragma unroll 1
                 for (int w = 0; w < NQ; w++) {
-                    const uint4 a = cb[warp][w];
-                    const uint4 b = tb[w][t];
-                    d += __popc(a.x & b.x) + __popc(a.y & b.y) + __popc(a.z & b.z) +
-                         __popc(a.w & b.w);
+                    const uint4 a1 = cb[w], b1 = tb[w * RG + t];
+                    const uint4 a2 = cb[NQ + w], b2 = tb[(NQ + w) * RG + t];
+                    d += __popc(a1.x & b1.x) + __popc(a1.y & b1.y) + __popc(a1.z & b1.z) +
+                         __popc(a1.w & b1.w);
+                    d += __popc(a2.x & b2.x) + __popc(a2.y & b2.y) + __popc(a2.z & b2.z) +
+                         __popc(a2.w & b2.w);
                 }
                 if ((ok_bits[h] >> lane) & 1u) {
                     n_wf++;
@@ -2013,16 +2041,23 @@ void launch_bfilter_idx_t(const DevReads& R, RoundBuffers& B, const int32_t* rem
 template <int K>
 void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
                            cudaStream_t s) {
+    // passes with one tentative (the first passes of adaptive R) go to the
+    // plain kernel, which streams the candidates against one table
+    launch_filter_t<K, false>(R, B, remain, s, B.tent);
     const int xsmem = (kFilterThreads / 32) * (1 << (2 * K)) * 2;
+    constexpr int bsmem = (int)BitsSmem<K>::bytes;
     static int grid = 0, xgrid = 0;
     if (!grid) {
+        cudaFuncSetAttribute(k_bfilter_bits<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bsmem);
         cudaFuncSetAttribute(k_bexact<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, xsmem);
-        grid = grid_for(k_bfilter_bits<K>, kFilterThreads, 0, 8);
+        grid = grid_for(k_bfilter_bits<K>, kBitsThreads, bsmem, 2);
         xgrid = grid_for(k_bexact<K>, kFilterThreads, xsmem, 8);
     }
-    k_bfilter_bits<K><<<shaped(grid, R.filter_blocks), kFilterThreads, 0, s>>>(R, B.st, remain, B.tent, B.pairs, B.seg_cap,
-                                                      B.amb);
-    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kFilterThreads, xsmem, s>>>(R, B.st, B.amb, B.pairs, B.seg_cap);
+    k_bfilter_bits<K><<<shaped(grid, R.filter_blocks), kBitsThreads, bsmem, s>>>(
+        R, B.st, remain, B.tent, B.pairs, B.seg_cap, B.amb);
+    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kFilterThreads, xsmem, s>>>(R, B.st, B.amb,
+                                                                             B.pairs, B.seg_cap);
 }
 
 template <bool BATCH>
@@ -2254,7 +2289,7 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     if (ev4) cudaEventRecordWithFlags(ev4[3], s, cudaEventRecordExternal);
     if (count)
         *count += 8 + align_launches<true>(B) + (!drop ? 1 : 0) +
-                  (R.pig_q && !drop ? 1 : 0);
+                  (R.pig_q && !drop ? 1 : 0) + (B.amb && !drop ? 1 : 0);
 }
 
 // Whether a job's per-pass k-mer index (at most `cap` postings) is kept in
