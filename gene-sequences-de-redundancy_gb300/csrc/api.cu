@@ -224,7 +224,9 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     // 16-byte copies read whole: both rounded up to 8 entries
     B.idx_off16 = P.idx_smem ? c.take<uint16_t>(((size_t)1 << (2 * k)) + 8) : nullptr;
     B.idx_post16 = P.idx_smem ? c.take<uint16_t>((size_t)P.idx_cap + 8) : nullptr;
-    B.amb = P.bits ? c.take<Pair>((size_t)B.seg_cap) : nullptr;
+    // (four alignment queues' worth: a pass whose open pairs overflow it is redone)
+    B.amb_cap = P.bits ? 4 * B.seg_cap : 0;
+    B.amb = P.bits ? c.take<Pair>((size_t)B.amb_cap) : nullptr;
     // word lengths 8..12: k-mer ids and counts apart, the global table, the
     // per-CTA hash scratch (slots: a power of two >= 2 x the longest read)
     const bool wide = !drop && k >= kWideK;

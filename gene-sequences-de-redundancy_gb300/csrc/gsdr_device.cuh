@@ -203,7 +203,8 @@ struct RoundBuffers {
     int32_t r_max;       // largest R of the job (sizes the index filter's shared memory)
     // batched word filter by k-mer presence bitmaps (k <= kMaxBitsK; null =
     // another form): pairs the bound D <= S <= D + min(excess) cannot decide
-    Pair* amb;           // seg_cap pairs
+    Pair* amb;           // amb_cap pairs
+    int32_t amb_cap;
 };
 void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
                  int pass_limit = 0);

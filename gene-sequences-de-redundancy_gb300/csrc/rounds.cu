@@ -1254,7 +1254,8 @@ template <int K>
 __global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, RoundState* st,
                                                                   const int32_t* __restrict__ remain,
                                                                   const int32_t* __restrict__ tent,
-                                                                  Pair* pairs, int seg_cap, Pair* amb) {
+                                                                  Pair* pairs, int seg_cap, Pair* amb,
+                                                                  int amb_cap) {
     using L = BitsSmem<K>;
     constexpr int NQ = L::NQ;
     constexpr int RG = kBitsGroup;
@@ -1346,7 +1347,7 @@ __global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, Ro
                         n_al++;
                     } else if (d + min(textra[t], exq) >= cw) {
                         const int slot = atomicAdd(&st->n_amb, 1);
-                        if (slot < seg_cap) amb[slot] = Pair{ttent[t], q};
+                        if (slot < amb_cap) amb[slot] = Pair{ttent[t], q};
                         else st->pair_overflow = 1;
                     }
                 }
@@ -1371,12 +1372,12 @@ __global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, Ro
 template <int K>
 __global__ void __launch_bounds__(kFilterThreads) k_bexact(DevReads R, RoundState* st,
                                                            const Pair* __restrict__ amb,
-                                                           Pair* pairs, int seg_cap) {
+                                                           int amb_cap, Pair* pairs, int seg_cap) {
     constexpr int NB = 1 << (2 * K);
     constexpr int WARPS = kFilterThreads / 32;
     extern __shared__ __align__(16) uint16_t xtab[];  // [WARPS][NB]
     if (st->done || st->n_tent == 0) return;
-    const int na = min(st->n_amb, seg_cap);
+    const int na = min(st->n_amb, amb_cap);
     if (na <= 0) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint16_t* tab = xtab + warp * NB;
@@ -1792,7 +1793,7 @@ __global__ void k_bapply(RoundState* st, const Pair* __restrict__ acc,
 }
 
 __global__ void k_badvance(RoundState* st, const int32_t* __restrict__ tent, int* align_work,
-                           int seg_cap, int acc_cap, int drop) {
+                           int seg_cap, int acc_cap, int amb_cap, int drop) {
     if (st->done) return;
     st->passes += 1;
     st->pass += 1;
@@ -1836,6 +1837,9 @@ __global__ void k_badvance(RoundState* st, const int32_t* __restrict__ tent, int
         // and a small R)
         if (nt > 0 && fullest > 0) r = min(r, (long long)nt * (3ll * seg_cap / 4) / fullest);
         if (nt > 0 && st->n_acc > 0) r = min(r, (long long)nt * (3ll * acc_cap / 4) / st->n_acc);
+        // and the bitmap filter's queue of open pairs
+        if (nt > 0 && amb_cap > 0 && st->n_amb > 0)
+            r = min(r, (long long)nt * (3ll * amb_cap / 4) / st->n_amb);
         st->R = (int)max(1ll, min((long long)st->R_max, r));
     }
     const int n = st->n_next;
@@ -2055,9 +2059,9 @@ void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* re
         xgrid = grid_for(k_bexact<K>, kFilterThreads, xsmem, 8);
     }
     k_bfilter_bits<K><<<shaped(grid, R.filter_blocks), kBitsThreads, bsmem, s>>>(
-        R, B.st, remain, B.tent, B.pairs, B.seg_cap, B.amb);
-    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kFilterThreads, xsmem, s>>>(R, B.st, B.amb,
-                                                                             B.pairs, B.seg_cap);
+        R, B.st, remain, B.tent, B.pairs, B.seg_cap, B.amb, B.amb_cap);
+    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kFilterThreads, xsmem, s>>>(
+        R, B.st, B.amb, B.amb_cap, B.pairs, B.seg_cap);
 }
 
 template <bool BATCH>
@@ -2285,7 +2289,8 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     k_bclaim<<<g, 256, 0, s>>>(B.st, B.acc, B.tidx, B.survive, B.best);
     k_bapply<<<g, 256, 0, s>>>(B.st, B.acc, B.tidx, B.best, B.cluster);
     k_compact<<<num_sms() * 4, 256, 0, s>>>(B.st, rin, rout, B.cluster);
-    k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st), B.seg_cap, B.acc_cap, drop);
+    k_badvance<<<1, 1, 0, s>>>(B.st, B.tent, align_work_of(B.st), B.seg_cap, B.acc_cap,
+                               B.amb_cap, drop);
     if (ev4) cudaEventRecordWithFlags(ev4[3], s, cudaEventRecordExternal);
     if (count)
         *count += 8 + align_launches<true>(B) + (!drop ? 1 : 0) +
