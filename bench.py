@@ -179,7 +179,8 @@ def filter_roofline(r, figures):
     kernel = {"table": "k_bfilter_tab (per-tentative k-mer tables in shared memory, "
                        "transposed, paired 16-bit min/add)",
               "index": "k_bindex + k_bfilter_idx (inverted k-mer index in shared memory)",
-              "bits": "k_bfilter_bits + k_bexact (k-mer presence bitmaps)"}[form]
+              "bits": "k_bfilter_bits + k_bexact (two-level k-mer count bitmaps: AND + POPC "
+                      "per tentative, exact sums for the pairs the bound leaves open)"}[form]
     ratio = figures.get("c%d.filter_%s.dram_over_input" % (r["config"], form))
     return {"bound": "hbm", "kernel": kernel,
             "achieved": achieved, "peak": r["peak"], "unit": "GB/s",
@@ -206,6 +207,12 @@ def measured_filter_bound(form, figures):
                 "bank_conflict_wavefront_share": figures.get(
                     "c1.filter_table.bank_conflict_wavefront_share"),
                 "source": "profiles/k_bfilter_tab_c1_smem.md (200k-read workload)"}
+    if form == "bits" and figures.get("c1.filter_bits.alu_pipe_pct") is not None:
+        return {"resource": "integer pipes (AND + POPC)", "kernel": "k_bfilter_bits<6>",
+                "alu_pipe_pct": figures["c1.filter_bits.alu_pipe_pct"],
+                "ipc_of_4": figures.get("c1.filter_bits.ipc"),
+                "dram_pct_of_peak": figures.get("c1.filter_bits.dram_pct"),
+                "source": "profiles/k_bfilter_bits_c1.md (200k-read workload)"}
     if form == "index" and figures.get("c2.filter_index.ipc") is not None:
         return {"resource": "instruction issue", "kernel": "k_bfilter_idx<7>",
                 "ipc_of_4": figures["c2.filter_index.ipc"],

@@ -132,10 +132,12 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
     }
     if (o.batch != 1 && !drop && n > 0 && k < kWideK) {
         bool index = ents_sum * kIndexDensity <= kcap * (int64_t)n;
-        // the bitmap bound decides almost every pair of short reads but
-        // almost none once reads hold most of the 4^k k-mers (long reads at
-        // k = 6): automatic only below a quarter of the k-mer space
-        bool bits = !index && k <= kMaxBitsK && ents_sum * 4 <= kcap * (int64_t)n;
+        // k <= 6: the two-level count bitmaps (measured faster than the
+        // tables on every workload tried: 200k reads of 300-10,000 bp 50.2
+        // against 53.3 ms, jobs of 150-5,000 bp 0.90 against 3.96 s at 200k
+        // reads and 82 against 298 ms at 50k, 10k reads of 200-1,000 bp 7.0
+        // against 8.4 ms)
+        bool bits = !index && k <= kMaxBitsK;
         // the caller's choice (word_filter), else GSDR_BFILTER=table|index|bits
         int form = o.word_filter;
         if (form == 0) {

@@ -119,9 +119,17 @@ def test_c1_recipe_bits_forced(tmp_path, monkeypatch, batch):
     assert st.k == 6 and st.word_index == 2
 
 
-def test_c1_recipe_tables_auto(tmp_path, monkeypatch):
+def test_c1_recipe_bits_auto(tmp_path, monkeypatch):
+    # long reads too: the two-level bitmaps are the automatic form for k <= 6
     data = gsdr.synth_fasta(1, n_reads=8000, seed=41)
     st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 0, None)
+    assert st.k == 6 and st.word_index == 2
+
+
+@pytest.mark.parametrize("batch", [2, 256])
+def test_c1_recipe_tables_forced(tmp_path, monkeypatch, batch):
+    data = gsdr.synth_fasta(1, n_reads=8000, seed=41)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, batch, "table")
     assert st.k == 6 and st.word_index == 0
 
 
