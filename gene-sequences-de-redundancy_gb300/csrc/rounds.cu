@@ -147,7 +147,7 @@ __device__ __forceinline__ unsigned long long cand_bytes(const DevReads& R, int 
 // smallest unclustered read, so every other remaining read is its candidate
 // and the pass is a plain round; k_bfilter_tab takes the passes with more.
 template <int K, bool DROP>
-__global__ void __launch_bounds__(kFilterThreads, 5) k_filter(DevReads R, RoundState* st,
+__global__ void __launch_bounds__(kFilterThreads, 6) k_filter(DevReads R, RoundState* st,
                                                            const int32_t* __restrict__ remain,
                                                            Pair* pairs, int seg_cap,
                                                            const int32_t* __restrict__ tent) {
@@ -186,35 +186,30 @@ __global__ void __launch_bounds__(kFilterThreads, 5) k_filter(DevReads R, RoundS
     unsigned long long bytes = 0;
     const int nwarps = gridDim.x * (kFilterThreads / 32);
     // Software pipeline over this warp's candidates: while candidate i is
-    // decided, the composition, cutoff and k-mer bitmap of candidate i+1 are
-    // already in flight and the index of candidate i+2 too, so the chain of
-    // dependent loads (remain -> scalars and bitmap -> list) overlaps the
-    // previous candidate's list stream instead of stalling the warp once per
-    // candidate (48 registers: five CTAs per SM).
+    // decided, the composition and cutoff of candidate i+1 are already in
+    // flight and the index of candidate i+2 too, so part of the chain of
+    // dependent loads (remain -> scalars -> list) overlaps the previous
+    // candidate's list stream.  (Prefetching the bitmap as well needs 48
+    // registers, five CTAs per SM instead of six, and measured slower.)
     int idx = blockIdx.x * (kFilterThreads / 32) + (threadIdx.x >> 5);
     int q_nx = idx < n ? __ldg(remain + idx) : -1;
     int q_af = idx + nwarps < n ? __ldg(remain + idx + nwarps) : -1;
     int4 comp_nx = make_int4(0, 0, 0, 0);
     int cb_nx = 0;
-    uint4 bits_nx = make_uint4(0u, 0u, 0u, 0u);  // the candidate's bitmap, one quad per lane
-    const uint4* kb4 = BITS ? reinterpret_cast<const uint4*>(R.kbits) : nullptr;
     if (q_nx >= 0) {
         comp_nx = R.comp[q_nx];
         cb_nx = R.cut_base[q_nx];
-        if (BITS) bits_nx = __ldcs(kb4 + (size_t)q_nx * (NBW / 4) + lane % (NBW / 4));
     }
     for (; idx < n; idx += nwarps) {
         const int q = q_nx;
         const int4 comp_q = comp_nx;
         const int cb_q = cb_nx;
-        const uint4 cb = bits_nx;
         // issue the next candidate's loads before this one's work
         q_nx = q_af;
         q_af = idx + 2 * nwarps < n ? __ldg(remain + idx + 2 * nwarps) : -1;
         if (q_nx >= 0) {
             comp_nx = R.comp[q_nx];
             cb_nx = R.cut_base[q_nx];
-            if (BITS) bits_nx = __ldcs(kb4 + (size_t)q_nx * (NBW / 4) + lane % (NBW / 4));
         }
         if (q == rep) continue;
         n_pf++;
@@ -234,6 +229,7 @@ __global__ void __launch_bounds__(kFilterThreads, 5) k_filter(DevReads R, RoundS
                 // D = shared k-mers (non-zero counts) bounds S: D <= S <= D + min(excesses)
                 bytes += 4ull * NBW;
                 const int q_extra = R.kextra[q];
+                const uint4 cb = __ldcs(reinterpret_cast<const uint4*>(R.kbits + (size_t)q * NBW) + lane % (NBW / 4));
                 int d = 0;
                 if (lane < NBW / 4) {
                     const uint4 rb = reinterpret_cast<const uint4*>(rbits)[lane];
@@ -1525,9 +1521,6 @@ __global__ void __launch_bounds__(kIndexThreads, 1) k_bindex(DevReads R, RoundSt
 // from the 32-bit list"); otherwise the 32-bit offsets only.  Then the
 // tentatives, and per warp the 16-bit sums (two per word).
 constexpr int kIdxGroups = 8;  // groups of 32 k-mer entries held in registers at a time
-// longest posting list of a group of 32 k-mers up to which each lane walks its
-// own list (above it the group's postings are spread evenly over the lanes)
-constexpr uint32_t kIdxLaneWalk = 12;
 struct IndexSmem {
     int off_words, post_words, tent_words, acc_words;
     __host__ __device__ IndexSmem(int k, int r_max, long long cap, bool smem_index) {
@@ -1629,33 +1622,6 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
                 const uint32_t c = v & 0xffffu;
                 const uint32_t s0 = SMEM ? s_off16[km] : s_off32[km];
                 const uint32_t sz = c ? (SMEM ? s_off16[km + 1] : s_off32[km + 1]) - s0 : 0u;
-                // Short lists (the usual case: a k-mer is held by a few of the
-                // pass's tentatives): every lane walks its own k-mer's list and
-                // the warp runs as many steps as the longest one, a handful of
-                // instructions per step.  A group with a long list (a common
-                // k-mer) is balanced over the lanes below instead.
-                const uint32_t longest = __reduce_max_sync(kFull, sz);
-                if (longest <= kIdxLaneWalk) {
-                    for (uint32_t r = 0; r < longest; r++) {
-                        if (r < sz) {
-                            const uint32_t j = s0 + r;
-                            uint32_t t, ct;
-                            if (SMEM) {
-                                const uint32_t pp = s_post16[j];
-                                t = pp >> 6;
-                                ct = pp & 63u;
-                                if (ct == 63u) ct = __ldg(idx_post + j) & 0xffffu;
-                            } else {
-                                const uint32_t pp = __ldg(idx_post + j);
-                                t = pp >> 16;
-                                ct = pp & 0xffffu;
-                            }
-                            if (t < (uint32_t)ntq)
-                                atomicAdd(&acc[t >> 1], min(ct, c) << ((t & 1u) << 4));
-                        }
-                    }
-                    continue;
-                }
                 uint32_t incl = sz;
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
