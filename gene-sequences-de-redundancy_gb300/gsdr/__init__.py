@@ -452,11 +452,35 @@ def _host_bytes(data):
     return C.c_void_p(a.ctypes.data), a.nbytes
 
 
-def cluster_fasta(data, opts: Opts | None = None, stats: bool = False, **kw):
+class _Result:
+    """Owns a gsdr_result; views over its buffers keep it alive."""
+
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        if self.h:
+            lib().gsdr_result_free(self.h)
+            self.h = None
+
+
+def _view(owner, addr, n, ctype, dtype):
+    """A numpy array over n ctype items at addr that keeps `owner` alive."""
+    if n == 0:
+        return np.empty(0, dtype=dtype)
+    buf = (ctype * n).from_address(addr)
+    buf._owner = owner
+    return np.frombuffer(buf, dtype=dtype)
+
+
+def cluster_fasta(data, opts: Opts | None = None, stats: bool = False, copy: bool = True,
+                  **kw):
     """readFile + clustering + saveFile on the device (gsdr_cluster_fasta):
     FASTA bytes in (bytes, or a uint8 array such as a view of pinned host
     memory); returns (output FASTA bytes, cluster[] in sorted order, the sort
-    permutation), and the Stats when stats=True."""
+    permutation), and the Stats when stats=True.  copy=False returns the output
+    as a uint8 array and the two int32 arrays as views of the library's result
+    buffers (no host copy; the result lives as long as any of them)."""
     o = opts if opts is not None else default_opts()
     for k, v in kw.items():
         setattr(o, k, v)
@@ -464,6 +488,15 @@ def cluster_fasta(data, opts: Opts | None = None, stats: bool = False, **kw):
     h = C.c_void_p()
     ptr, size = _host_bytes(data)
     _check(lib().gsdr_cluster_fasta(ptr, size, C.byref(o), C.byref(h), C.byref(st)))
+    if not copy:
+        res = _Result(h)
+        p, n = C.c_void_p(), C.c_int64()
+        _check(lib().gsdr_result_output(h, C.byref(p), C.byref(n)))
+        cnt = lib().gsdr_result_count(h)
+        out = _view(res, p.value or 0, n.value, C.c_uint8, np.uint8)
+        cl = _view(res, lib().gsdr_result_cluster(h) or 0, cnt, C.c_int32, np.int32)
+        order = _view(res, lib().gsdr_result_order(h) or 0, cnt, C.c_int32, np.int32)
+        return (out, cl, order, st) if stats else (out, cl, order)
     try:
         ptr, n = C.c_void_p(), C.c_int64()
         _check(lib().gsdr_result_output(h, C.byref(ptr), C.byref(n)))

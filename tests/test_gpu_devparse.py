@@ -101,3 +101,20 @@ def test_device_parse_large_ties_match_std_sort(tmp_path):
     np.testing.assert_array_equal(order, oorder)
     np.testing.assert_array_equal(horder, oorder)
     assert out == hout
+
+
+def test_zero_copy_result_views_outlive_the_call():
+    # copy=False: output and arrays are views of the library's result buffers;
+    # they stay valid while any of them is referenced
+    import gc
+
+    data = gsdr.synth_fasta(0, n_reads=2000, seed=74)
+    out, cl, order = gsdr.cluster_fasta(data, threshold=0.95)
+    vout, vcl, vorder = gsdr.cluster_fasta(data, threshold=0.95, copy=False)
+    del vout, vorder
+    gc.collect()
+    np.testing.assert_array_equal(vcl, cl)
+    vout, _, vorder = gsdr.cluster_fasta(data, threshold=0.95, copy=False)
+    gc.collect()
+    assert vout.dtype == np.uint8 and vout.tobytes() == out
+    np.testing.assert_array_equal(vorder, order)
