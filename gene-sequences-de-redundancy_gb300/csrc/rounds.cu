@@ -1327,20 +1327,30 @@ __global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, Ro
             __syncwarp();
             const int cw = R.cut_word[q];
             const int exq = R.kextra3[q];
+            // word by word: the candidate's two quads load once and serve every
+            // chunk of 32 tentatives with a pair left (fewer shared loads: the
+            // kernel is bound by their issue queue and the POPC pipe)
+            int dsum[RG / 32];
+#pragma unroll
+            for (int h = 0; h < RG / 32; h++) dsum[h] = 0;
+#pragma unroll 1
+            for (int w = 0; w < NQ; w++) {
+                const uint4 a1 = cb[w], a2 = cb[NQ + w];
+#pragma unroll
+                for (int h = 0; h < RG / 32; h++) {
+                    if (!ok_bits[h]) continue;
+                    const int t = 32 * h + lane;
+                    const uint4 b1 = tb[w * RG + t], b2 = tb[(NQ + w) * RG + t];
+                    dsum[h] += __popc(a1.x & b1.x) + __popc(a1.y & b1.y) + __popc(a1.z & b1.z) +
+                               __popc(a1.w & b1.w) + __popc(a2.x & b2.x) + __popc(a2.y & b2.y) +
+                               __popc(a2.z & b2.z) + __popc(a2.w & b2.w);
+                }
+            }
 #pragma unroll
             for (int h = 0; h < RG / 32; h++) {
                 if (!ok_bits[h]) continue;
                 const int t = 32 * h + lane;
-                int d = 0;
-#pragma unroll 1
-                for (int w = 0; w < NQ; w++) {
-                    const uint4 a1 = cb[w], b1 = tb[w * RG + t];
-                    const uint4 a2 = cb[NQ + w], b2 = tb[(NQ + w) * RG + t];
-                    d += __popc(a1.x & b1.x) + __popc(a1.y & b1.y) + __popc(a1.z & b1.z) +
-                         __popc(a1.w & b1.w);
-                    d += __popc(a2.x & b2.x) + __popc(a2.y & b2.y) + __popc(a2.z & b2.z) +
-                         __popc(a2.w & b2.w);
-                }
+                const int d = dsum[h];
                 if ((ok_bits[h] >> lane) & 1u) {
                     n_wf++;
                     if (d >= cw) {
