@@ -137,7 +137,7 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
         // against 53.3 ms, jobs of 150-5,000 bp 0.90 against 3.96 s at 200k
         // reads and 82 against 298 ms at 50k, 10k reads of 200-1,000 bp 7.0
         // against 8.4 ms)
-        bool bits = !index && k <= kMaxBitsK;
+        bool bits = !index && k <= kMaxBits2K;
         // the caller's choice (word_filter), else GSDR_BFILTER=table|index|bits
         int form = o.word_filter;
         if (form == 0) {
@@ -148,7 +148,7 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
         }
         if (form == 1) index = false, bits = false;
         if (form == 2) index = true, bits = false;
-        if (form == 3) index = false, bits = k <= kMaxBitsK;
+        if (form == 3) index = false, bits = k <= kMaxBits2K;
         P.bits = bits;
         // automatic R with the table and bitmap forms: the largest R (the
         // table form measured fastest at R_max 1024 on the 200k-read
@@ -199,7 +199,9 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     R.variant = P.variant;
     R.strict = P.variant == 1 ? 1 : 0;
     R.brk = P.variant == 1 && !drop ? c.take<uint32_t>((size_t)P.pack_off[n] + 8) : nullptr;
-    const bool bits = !drop && k <= kMaxBitsK;
+    // presence bitmaps: for the plain filter's bound (k <= 6) and for the
+    // batched two-level filter (k <= 7)
+    const bool bits = !drop && (k <= kMaxBitsK || P.bits);
     const size_t nbw = bits ? ((size_t)1 << (2 * k)) / 32 : 0;
     R.kbits = bits ? c.take<uint32_t>((size_t)n * nbw) : nullptr;
     R.kextra = bits ? c.take<int32_t>(n) : nullptr;

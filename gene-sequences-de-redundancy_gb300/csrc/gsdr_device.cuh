@@ -38,6 +38,7 @@ __host__ __device__ __forceinline__ int group_class(int bw) {
 constexpr int kMaxBatch = 1024;         // tentative representatives per batched pass
 constexpr int kTTWords = kMaxBatch / 32;
 constexpr int kMaxBitsK = 6;            // k-mer presence bitmaps for k <= 6 (4^k bits per read)
+constexpr int kMaxBits2K = 7;           // the batched two-level bitmap filter: k <= 7
 
 struct Pair {
     int32_t rep;   // read index of the representative (or tentative)

@@ -189,13 +189,16 @@ __device__ __forceinline__ bool window_broken(const uint32_t* brk, int p, int k)
 template <int K>
 __global__ void __launch_bounds__(256) k_kmers_hist(DevReads R) {
     constexpr int NB = 1 << (2 * K);
-    constexpr bool BITS = K <= kMaxBitsK;
-    constexpr int NBW = BITS ? NB / 32 : 1;
+    // presence bitmaps: k <= 6 always (the plain filter's bound), k = 7 only
+    // for the batched two-level filter (kbits allocated)
+    constexpr bool BITS_T = K <= kMaxBits2K;
+    constexpr int NBW = BITS_T ? NB / 32 : 1;
     extern __shared__ __align__(16) uint32_t sm[];
     uint32_t* hist = sm;
     uint16_t* list = reinterpret_cast<uint16_t*>(sm + NB);
     __shared__ uint32_t bits[NBW], bits2[NBW];
     __shared__ int nlist, sumcnt, sum3;
+    const bool BITS = BITS_T && R.kbits != nullptr;
     const bool level2 = BITS && R.kbits2 != nullptr;
     for (int i = threadIdx.x; i < NB; i += blockDim.x) hist[i] = 0;
     for (int i = threadIdx.x; i < NBW; i += blockDim.x) bits[i] = bits2[i] = 0;

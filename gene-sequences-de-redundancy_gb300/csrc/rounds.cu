@@ -1235,31 +1235,51 @@ __global__ void __launch_bounds__(kFilterThreads) k_bprefilter(DevReads R, Round
 // keeps the gap small where one level leaves it wide (reads holding a large
 // share of the k-mer space, whose counts are mostly 1 or 2).
 
-constexpr int kBitsGroup = 128;    // tentatives staged per CTA
-constexpr int kBitsThreads = 1024;
+// Carry-save adder: a + b + c = s + 2 * carry, bit by bit (two LOP3s).
+__device__ __forceinline__ void csa(uint32_t& s, uint32_t& carry, uint32_t a, uint32_t b,
+                                    uint32_t c) {
+    s = a ^ b ^ c;
+    carry = (a & b) | (c & (a ^ b));
+}
+
+// The summed population count of eight words with four POPCs (the POPC pipe
+// bounds the bitmap filter): a tree of carry-save adders (Harley and Seal)
+// reduces them to words of weight 1, 1, 2 and 4 first.
+__device__ __forceinline__ int popc8(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
+                                     uint32_t w4, uint32_t w5, uint32_t w6, uint32_t w7) {
+    uint32_t s1, c1, s2, c2, s3, c3, t2, f4;
+    csa(s1, c1, w0, w1, w2);
+    csa(s2, c2, w3, w4, w5);
+    csa(s3, c3, s1, s2, w6);
+    csa(t2, f4, c1, c2, c3);
+    return __popc(s3) + __popc(w7) + 2 * __popc(t2) + 4 * __popc(f4);
+}
 
 // Shared memory of k_bfilter_bits: the group's two bitmap levels as
 // [level][quad][tentative] (lane t reads consecutive 16 bytes: conflict-free),
 // each warp's candidate bitmaps, and the group's tentatives, compositions and
-// excesses.
+// excesses.  k <= 6: 128 tentatives per CTA of 32 warps (163 KB); k = 7, whose
+// bitmaps are four times larger: 32 tentatives per CTA of 16 warps (193 KB).
 template <int K>
 struct BitsSmem {
     static constexpr int NQ = (1 << (2 * K)) / 128;  // 16-byte words of one bitmap
-    static constexpr int WARPS = kBitsThreads / 32;
-    static constexpr size_t tb_quads = 2 * (size_t)NQ * kBitsGroup;
+    static constexpr int RG = K <= 6 ? 128 : 32;     // tentatives staged per CTA
+    static constexpr int THREADS = K <= 6 ? 1024 : 512;
+    static constexpr int WARPS = THREADS / 32;
+    static constexpr size_t tb_quads = 2 * (size_t)NQ * RG;
     static constexpr size_t cb_quads = (size_t)WARPS * 2 * NQ;
-    static constexpr size_t bytes = 16 * (tb_quads + cb_quads) + kBitsGroup * (16 + 4 + 4);
+    static constexpr size_t bytes = 16 * (tb_quads + cb_quads) + RG * (16 + 4 + 4);
 };
 
 template <int K>
-__global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, RoundState* st,
+__global__ void __launch_bounds__(BitsSmem<K>::THREADS, 1) k_bfilter_bits(DevReads R, RoundState* st,
                                                                   const int32_t* __restrict__ remain,
                                                                   const int32_t* __restrict__ tent,
                                                                   Pair* pairs, int seg_cap, Pair* amb,
                                                                   int amb_cap) {
     using L = BitsSmem<K>;
     constexpr int NQ = L::NQ;
-    constexpr int RG = kBitsGroup;
+    constexpr int RG = L::RG;
     constexpr int WARPS = L::WARPS;
     extern __shared__ __align__(16) uint4 bsm[];
     uint4* tb = bsm;                                  // tb[(level * NQ + w) * RG + t]
@@ -1293,7 +1313,7 @@ __global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, Ro
                 tcomp[threadIdx.x] = in ? R.comp[rep] : make_int4(0, 0, 0, 0);
                 textra[threadIdx.x] = in ? R.kextra3[rep] : 0;
             }
-            for (int i = threadIdx.x; i < 2 * NQ * RG; i += kBitsThreads) {
+            for (int i = threadIdx.x; i < 2 * NQ * RG; i += L::THREADS) {
                 const int t = i % RG, lw = i / RG, lv = lw / NQ, w = lw % NQ;
                 uint4 v = make_uint4(0u, 0u, 0u, 0u);
                 if (t < ng) v = __ldg((lv ? kb2 : kb1) + (size_t)tent[t0 + t] * NQ + w);
@@ -1341,9 +1361,8 @@ __global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, Ro
                     if (!ok_bits[h]) continue;
                     const int t = 32 * h + lane;
                     const uint4 b1 = tb[w * RG + t], b2 = tb[(NQ + w) * RG + t];
-                    dsum[h] += __popc(a1.x & b1.x) + __popc(a1.y & b1.y) + __popc(a1.z & b1.z) +
-                               __popc(a1.w & b1.w) + __popc(a2.x & b2.x) + __popc(a2.y & b2.y) +
-                               __popc(a2.z & b2.z) + __popc(a2.w & b2.w);
+                    dsum[h] += popc8(a1.x & b1.x, a1.y & b1.y, a1.z & b1.z, a1.w & b1.w,
+                                     a2.x & b2.x, a2.y & b2.y, a2.z & b2.z, a2.w & b2.w);
                 }
             }
 #pragma unroll
@@ -1379,13 +1398,17 @@ __global__ void __launch_bounds__(kBitsThreads, 1) k_bfilter_bits(DevReads R, Ro
 
 // The word sum S itself for the pairs k_bfilter_bits left open: one warp per
 // pair scatters the tentative's counts into a table in shared memory and
-// streams the candidate's (k-mer, count) entries against it.
+// streams the candidate's (k-mer, count) entries against it.  (k = 7: tables
+// of 32 KB, four warps per CTA.)
 template <int K>
-__global__ void __launch_bounds__(kFilterThreads) k_bexact(DevReads R, RoundState* st,
+constexpr int kExactThreads = K <= 6 ? kFilterThreads : 128;
+
+template <int K>
+__global__ void __launch_bounds__(kExactThreads<K>) k_bexact(DevReads R, RoundState* st,
                                                            const Pair* __restrict__ amb,
                                                            int amb_cap, Pair* pairs, int seg_cap) {
     constexpr int NB = 1 << (2 * K);
-    constexpr int WARPS = kFilterThreads / 32;
+    constexpr int WARPS = kExactThreads<K> / 32;  // one NB-entry table each
     extern __shared__ __align__(16) uint16_t xtab[];  // [WARPS][NB]
     if (st->done || st->n_tent == 0) return;
     const int na = min(st->n_amb, amb_cap);
@@ -2059,19 +2082,20 @@ void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* re
     // passes with one tentative (the first passes of adaptive R) go to the
     // plain kernel, which streams the candidates against one table
     launch_filter_t<K, false>(R, B, remain, s, B.tent);
-    const int xsmem = (kFilterThreads / 32) * (1 << (2 * K)) * 2;
+    constexpr int xsmem = (kExactThreads<K> / 32) * (1 << (2 * K)) * 2;
     constexpr int bsmem = (int)BitsSmem<K>::bytes;
+    constexpr int bthreads = BitsSmem<K>::THREADS;
     static int grid = 0, xgrid = 0;
     if (!grid) {
         cudaFuncSetAttribute(k_bfilter_bits<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              bsmem);
         cudaFuncSetAttribute(k_bexact<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, xsmem);
-        grid = grid_for(k_bfilter_bits<K>, kBitsThreads, bsmem, 2);
-        xgrid = grid_for(k_bexact<K>, kFilterThreads, xsmem, 8);
+        grid = grid_for(k_bfilter_bits<K>, bthreads, bsmem, 2);
+        xgrid = grid_for(k_bexact<K>, kExactThreads<K>, xsmem, 8);
     }
-    k_bfilter_bits<K><<<shaped(grid, R.filter_blocks), kBitsThreads, bsmem, s>>>(
+    k_bfilter_bits<K><<<shaped(grid, R.filter_blocks), bthreads, bsmem, s>>>(
         R, B.st, remain, B.tent, B.pairs, B.seg_cap, B.amb, B.amb_cap);
-    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kFilterThreads, xsmem, s>>>(
+    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kExactThreads<K>, xsmem, s>>>(
         R, B.st, B.amb, B.amb_cap, B.pairs, B.seg_cap);
 }
 
@@ -2090,7 +2114,8 @@ void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain
         switch (R.k) {
             case 4: launch_bfilter_bits_t<4>(R, B, remain, s); break;
             case 5: launch_bfilter_bits_t<5>(R, B, remain, s); break;
-            default: launch_bfilter_bits_t<6>(R, B, remain, s); break;
+            case 6: launch_bfilter_bits_t<6>(R, B, remain, s); break;
+            default: launch_bfilter_bits_t<7>(R, B, remain, s); break;
         }
         return;
     }

@@ -133,11 +133,20 @@ def test_c1_recipe_tables_forced(tmp_path, monkeypatch, batch):
     assert st.k == 6 and st.word_index == 0
 
 
-@pytest.mark.parametrize("w", [4, 5, 6])
+@pytest.mark.parametrize("w", [4, 5, 6, 7])
 def test_bits_word_lengths(tmp_path, monkeypatch, w):
     data = gsdr.synth_fasta(0, n_reads=2000, seed=42)
     st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 64, "bits", w=w)
     assert st.k == w and st.word_index == 2
+
+
+@pytest.mark.parametrize("batch", [32, 0])
+def test_bits_k7_long_reads(tmp_path, monkeypatch, batch):
+    # t = 0.90 gives k = 7; reads of 150-5000 bp hold too many 7-mers for the
+    # index: the two-level bitmaps (four times larger at k = 7) are automatic
+    data = gsdr.synth_fasta(4, n_reads=3000, seed=45, n_seeds=600, len_lo=150, len_hi=5000)
+    st, ost = run_form(data, tmp_path, monkeypatch, 0.90, batch, None)
+    assert st.k == 7 and ost.k == 7 and st.word_index == 2
 
 
 @pytest.mark.parametrize("t", [0.88, 0.93, 0.97])
