@@ -208,7 +208,9 @@ def measured_filter_bound(form, figures):
                     "c1.filter_table.bank_conflict_wavefront_share"),
                 "source": "profiles/k_bfilter_tab_c1_smem.md (200k-read workload)"}
     if form == "bits" and figures.get("c1.filter_bits.alu_pipe_pct") is not None:
-        return {"resource": "integer pipes (AND + POPC)", "kernel": "k_bfilter_bits<6>",
+        return {"resource": "POPC (XU) and ALU pipes", "kernel": "k_bfilter_bits<6>",
+                "sm_throughput_pct": figures.get("c1.filter_bits.sm_throughput_pct"),
+                "xu_pipe_pct": figures.get("c1.filter_bits.xu_pipe_pct"),
                 "alu_pipe_pct": figures["c1.filter_bits.alu_pipe_pct"],
                 "ipc_of_4": figures.get("c1.filter_bits.ipc"),
                 "dram_pct_of_peak": figures.get("c1.filter_bits.dram_pct"),

@@ -150,10 +150,13 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
         if (form == 2) index = true, bits = false;
         if (form == 3) index = false, bits = k <= kMaxBits2K;
         P.bits = bits;
-        // automatic R with the table and bitmap forms: the largest R (the
-        // table form measured fastest at R_max 1024 on the 200k-read
-        // workload: 22.6 us per representative against 25.5 at 256)
-        if (o.batch == 0 && !index) P.r_max = kMaxBatch;
+        // automatic R with the table and bitmap forms: the largest R for
+        // k <= 6 (the table form measured 22.6 us per representative at
+        // R_max 1024 against 25.5 at 256 on the 200k-read workload), 256 for
+        // k = 7, whose tables and bitmaps are four times larger (200k reads of
+        // 150-5,000 bp at t = 0.90: bitmaps 1.19 s at 256 against 1.72 s at
+        // 1024, tables 3.7 against 4.4 s)
+        if (o.batch == 0 && !index) P.r_max = k >= 7 ? 256 : kMaxBatch;
         if (index) {
             // a pass indexes at most R_max tentatives: for length-sorted reads
             // those hold at most the first R_max reads' entries
