@@ -546,46 +546,13 @@ __global__ void __launch_bounds__(kAlignThreads, 3) k_align(DevReads R, RoundSta
         const int T = R.len_gf[p.rep], q = R.len_gf[p.cand], c = R.cut_base[p.cand];
         const int trivial = trivial_decision(T, q, c);
         if (trivial < 0) {
-            // the pair's shape: B warps of wl words per lane, the fewest rows
-            // (B x 32 x wl words) that hold the pattern within the group's G
-            // warps, with W/2 < wl <= W (the widths compiled below), so a
-            // pattern just past a class boundary does not pay for a whole
-            // class of padding rows; the class's own shape is the fallback
             const int words = (q + 31) >> 5;
-            int B = (words + 32 * W - 1) / (32 * W), wl = W, best = B * W;
-#pragma unroll
-            for (int b = 1; b <= G; b++) {
-                const int w = (words + 32 * b - 1) / (32 * b);
-                if (w <= W && 2 * w > W && b * w < best) {
-                    best = b * w;
-                    B = b;
-                    wl = w;
-                }
-            }
-            if (gw < B) {
-                uint32_t* peq = peq_all + warp * sys_peq_words(W);
-                const uint32_t* pq = R.packed + R.pack_off[p.cand];
-                const uint32_t* pt = R.packed + R.pack_off[p.rep];
-                int blocks = 0;
-                switch (wl) {
-#define GSDR_SYS_CASE(n)                                                                       \
-    case n:                                                                                    \
-        if constexpr (W >= n && 2 * n > W)                                                     \
-            blocks = lcs_sys_pair<n>(S, peq, pq, q, pt, T, c, B, gw, lane, &st->error);        \
-        break;
-                    GSDR_SYS_CASE(1)
-                    GSDR_SYS_CASE(2)
-                    GSDR_SYS_CASE(3)
-                    GSDR_SYS_CASE(4)
-                    GSDR_SYS_CASE(5)
-                    GSDR_SYS_CASE(6)
-                    GSDR_SYS_CASE(7)
-                    GSDR_SYS_CASE(8)
-#undef GSDR_SYS_CASE
-                    default: break;
-                }
-                done += (unsigned long long)blocks * (32ull * 32 * 32) * wl;
-            }
+            const int B = (words + 32 * W - 1) / (32 * W);
+            if (gw < B)
+                done += (unsigned long long)lcs_sys_pair<W>(
+                            S, peq_all + warp * sys_peq_words(W), R.packed + R.pack_off[p.cand],
+                            q, R.packed + R.pack_off[p.rep], T, c, B, gw, lane, &st->error) *
+                        (32ull * 32 * 32 * W);
         }
         group_bar(bar_id, bar_n);
         if (gw == 0 && lane == 0) {
