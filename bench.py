@@ -175,12 +175,15 @@ def filter_roofline(r, figures):
     launches = max(1, r["filter_launches"])
     per_launch = r["filter_bytes"] / launches
     achieved = r["filter_gbs"]
-    form = {0: "table", 1: "index", 2: "bits"}.get(r["word_index"], "table")
+    form = {0: "table", 1: "index", 2: "bits", 3: "masks"}.get(r["word_index"], "table")
     kernel = {"table": "k_bfilter_tab (per-tentative k-mer tables in shared memory, "
                        "transposed, paired 16-bit min/add)",
               "index": "k_bindex + k_bfilter_idx (inverted k-mer index in shared memory)",
               "bits": "k_bfilter_bits + k_bexact (two-level k-mer count bitmaps: AND + POPC "
-                      "per tentative, exact sums for the pairs the bound leaves open)"}[form]
+                      "per tentative, exact sums for the pairs the bound leaves open)",
+              "masks": "k_bmask + k_bfilter_mask + k_bexact (per-k-mer rows of tentative bits "
+                       "in L2, bit-sliced counts per candidate, exact sums for the pairs the "
+                       "bound leaves open)"}[form]
     ratio = figures.get("c%d.filter_%s.dram_over_input" % (r["config"], form))
     return {"bound": "hbm", "kernel": kernel,
             "achieved": achieved, "peak": r["peak"], "unit": "GB/s",

@@ -72,6 +72,7 @@ struct Plan {
     int64_t idx_cap = 0;    // > 0: batched word filter by inverted index, postings capacity
     bool idx_smem = false;  // that index fits the filter's shared memory (16-bit copy)
     bool bits = false;      // batched word filter by k-mer presence bitmaps
+    bool masks = false;     // batched word filter by tentative masks
     // pigeon filter (p 1): low 16 bits of each read's offset in the
     // reference's padded layout (copyData, func.cu:119-137: L/16*16 + 16 per read)
     std::vector<uint16_t> refoff16;
@@ -138,25 +139,33 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
         // reads and 82 against 298 ms at 50k, 10k reads of 200-1,000 bp 7.0
         // against 8.4 ms)
         bool bits = !index && k <= kMaxBits2K;
-        // the caller's choice (word_filter), else GSDR_BFILTER=table|index|bits
+        // sparse spaces with short reads: the tentative masks, whose 8-plane
+        // counts hold reads of at most 255 k-mers
+        const bool masks_ok = k <= kMaxBits2K && ents_max <= kMaskMaxEntries;
+        bool masks = index && masks_ok;
+        // the caller's choice (word_filter), else GSDR_BFILTER=table|index|bits|masks
         int form = o.word_filter;
         if (form == 0) {
             const char* f = std::getenv("GSDR_BFILTER");
             if (f && std::strcmp(f, "table") == 0) form = 1;
             if (f && std::strcmp(f, "index") == 0) form = 2;
             if (f && std::strcmp(f, "bits") == 0) form = 3;
+            if (f && std::strcmp(f, "masks") == 0) form = 4;
         }
-        if (form == 1) index = false, bits = false;
-        if (form == 2) index = true, bits = false;
-        if (form == 3) index = false, bits = k <= kMaxBits2K;
+        if (form == 1) index = false, bits = false, masks = false;
+        if (form == 2) index = true, bits = false, masks = false;
+        if (form == 3) index = false, bits = k <= kMaxBits2K, masks = false;
+        if (form == 4 && masks_ok) index = false, bits = false, masks = true;
+        if (masks) index = false;
         P.bits = bits;
+        P.masks = masks;
         // automatic R with the table and bitmap forms: the largest R for
         // k <= 6 (the table form measured 22.6 us per representative at
         // R_max 1024 against 25.5 at 256 on the 200k-read workload), 256 for
         // k = 7, whose tables and bitmaps are four times larger (200k reads of
         // 150-5,000 bp at t = 0.90: bitmaps 1.19 s at 256 against 1.72 s at
         // 1024, tables 3.7 against 4.4 s)
-        if (o.batch == 0 && !index) P.r_max = k >= 7 ? 256 : kMaxBatch;
+        if (o.batch == 0 && !index) P.r_max = k >= 7 && !masks ? 256 : kMaxBatch;
         if (index) {
             // a pass indexes at most R_max tentatives: for length-sorted reads
             // those hold at most the first R_max reads' entries
@@ -232,8 +241,11 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     B.idx_off16 = P.idx_smem ? c.take<uint16_t>(((size_t)1 << (2 * k)) + 8) : nullptr;
     B.idx_post16 = P.idx_smem ? c.take<uint16_t>((size_t)P.idx_cap + 8) : nullptr;
     // (four alignment queues' worth: a pass whose open pairs overflow it is redone)
-    B.amb_cap = P.bits ? 4 * B.seg_cap : 0;
-    B.amb = P.bits ? c.take<Pair>((size_t)B.amb_cap) : nullptr;
+    B.amb_cap = P.bits || P.masks ? 4 * B.seg_cap : 0;
+    B.amb = P.bits || P.masks ? c.take<Pair>((size_t)B.amb_cap) : nullptr;
+    B.tmask_rwq = P.masks ? (P.r_max + 127) / 128 : 0;
+    B.tmask = P.masks ? c.take<uint4>(((size_t)1 << (2 * k)) * B.tmask_rwq) : nullptr;
+    B.tmask_ex = P.masks ? c.take<int32_t>(kMaxBatch) : nullptr;
     // word lengths 8..12: k-mer ids and counts apart, the global table, the
     // per-CTA hash scratch (slots: a power of two >= 2 x the longest read)
     const bool wide = !drop && k >= kWideK;
@@ -336,6 +348,7 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
         P.idx_cap = 0;
         P.idx_smem = false;
         P.bits = false;
+        P.masks = false;
     }
     r_max_ = P.r_max;
     stats.batch = batched_ ? r_max_ : 1;
@@ -362,7 +375,7 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
     JCUDA(dev_alloc(&dmem_, dbytes_, stream));
     carve_all(reinterpret_cast<char*>(dmem_), n, n_bytes_, P, opts.drop == 1, opts.word_length,
               R_, B_);
-    stats.word_index = P.idx_cap > 0 ? 1 : (P.bits ? 2 : 0);
+    stats.word_index = P.idx_cap > 0 ? 1 : P.bits ? 2 : P.masks ? 3 : 0;
     R_.threshold = opts.threshold;
     // band tiles of the banded alignment kernels (gsdr_opts; 0 = automatic,
     // where the environment may still override the defaults)

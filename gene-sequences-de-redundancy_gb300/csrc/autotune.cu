@@ -271,8 +271,10 @@ int autotune(const gsdr_reads* reads, const gsdr_opts* base_in, int reps, int ru
         t.o = o;
         t.stage = stage;
         run_trial(reads, t, reps, runs);
-        // a form the job could not take (bitmaps above word length 6) is not a setting
+        // a form the job could not take (bitmaps above word length 7, masks
+        // for reads above 255 k-mers) is not a setting
         if (t.ok && o.word_filter == 3 && t.word_index != 2) return;
+        if (t.ok && o.word_filter == 4 && t.word_index != 3) return;
         trials.push_back(t);
     };
     // stage 1: R_max x word-filter form (the form only matters with the filters on)
@@ -282,7 +284,7 @@ int autotune(const gsdr_reads* reads, const gsdr_opts* base_in, int reps, int ru
         o.word_filter = 0;
         run(o, "R x form");
         const int rs[] = {64, 256, 1024};
-        for (int form = drop ? 0 : 1; form <= (drop ? 0 : 3); form++)
+        for (int form = drop ? 0 : 1; form <= (drop ? 0 : 4); form++)
             for (int r : rs) {
                 o.batch = r;
                 o.word_filter = form;

@@ -339,8 +339,8 @@ int gsdr_resolve_opts(gsdr_opts* o, const char** msg) {
         m = "pigeon error (pigeon=0/1)";
     } else if (o->batch < 0) {
         m = "batch must be >= 0";
-    } else if (o->word_filter < 0 || o->word_filter > 3) {
-        m = "word filter form must be 0..3";
+    } else if (o->word_filter < 0 || o->word_filter > 4) {
+        m = "word filter form must be 0..4";
     } else if (o->variant != 0 && o->variant != 1) {
         m = "variant must be 0 (cuda-version) or 1 (SYCL program)";
     } else if (o->band_serial < -1) {

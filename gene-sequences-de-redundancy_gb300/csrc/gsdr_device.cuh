@@ -39,6 +39,7 @@ constexpr int kMaxBatch = 1024;         // tentative representatives per batched
 constexpr int kTTWords = kMaxBatch / 32;
 constexpr int kMaxBitsK = 6;            // k-mer presence bitmaps for k <= 6 (4^k bits per read)
 constexpr int kMaxBits2K = 7;           // the batched two-level bitmap filter: k <= 7
+constexpr int kMaskMaxEntries = 255;    // tentative-mask filter: reads of at most 255 k-mers
 
 struct Pair {
     int32_t rep;   // read index of the representative (or tentative)
@@ -202,10 +203,18 @@ struct RoundBuffers {
     uint16_t* idx_post16;
     int64_t idx_cap;
     int32_t r_max;       // largest R of the job (sizes the index filter's shared memory)
-    // batched word filter by k-mer presence bitmaps (k <= kMaxBitsK; null =
-    // another form): pairs the bound D <= S <= D + min(excess) cannot decide
+    // batched word filter by k-mer presence bitmaps or by tentative masks
+    // (null = another form): pairs the bound D <= S <= D + min(excess)
+    // cannot decide
     Pair* amb;           // amb_cap pairs
     int32_t amb_cap;
+    // batched word filter by tentative masks (short reads, k <= 7; null =
+    // another form): row m (tmask_rwq x 16 bytes) has bit t set iff tentative
+    // t holds k-mer m; tmask_ex[t] = its excess, sum of (count - 1).  Zeroed
+    // and rebuilt every pass.
+    uint4* tmask;        // 4^k rows
+    int32_t* tmask_ex;   // kMaxBatch
+    int32_t tmask_rwq;   // 16-byte words per row: ceil(r_max / 128)
 };
 void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
                  int pass_limit = 0);

@@ -1738,6 +1738,265 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
     }
 }
 
+// ---- word filter by tentative masks (short reads, sparse k-mer spaces) ----
+//
+// Per pass, for every k-mer m a row of R_max bits, bit t set iff tentative t
+// holds m with a non-zero count (k_bmask; 2 MB for k = 7 and R_max 1024, held
+// in L2).  One warp per candidate loads the rows of the candidate's k-mers, 16
+// bytes per lane, so one load instruction brings four rows of 1,024
+// tentatives, and counts per tentative the rows that have its bit:
+//     D1 = sum over k-mers of [c_t >= 1][c_q >= 1],
+// in bit-sliced counters (plane b holds bit b of 32 tentatives' counts) that
+// carry-save adders fill.  Since min(c_t, c_q) = [both >= 1] + (min - 1),
+//     D1 <= S <= D1 + min(E_t, E_q),   E = sum over k-mers of (count - 1),
+// so D1 >= cutoff passes a pair and D1 + min(E_t, E_q) < cutoff rejects it;
+// the pairs between go to k_bexact, which forms S itself.  Per pair the
+// kernel reads one bit per candidate k-mer and spends about one instruction
+// per 32 pairs and k-mer, where the index form walks every shared k-mer's
+// posting.  A count never exceeds the candidate's k-mer entries, so eight
+// planes hold it: the form runs only where every read has at most
+// kMaskMaxEntries entries.
+
+constexpr int kMaskThreads = 256;
+
+// One warp per tentative: sets the tentative's bit in the rows of its k-mers
+// (the rows were zeroed before) and writes its excess E_t.
+__global__ void __launch_bounds__(256) k_bmask(DevReads R, RoundState* st,
+                                               const int32_t* __restrict__ tent, uint32_t* tmask,
+                                               int32_t* tex, int rwq) {
+    if (st->done || st->n_tent == 0) return;
+    const int nt = st->n_tent;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const size_t row_words = 4 * (size_t)rwq;
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nw) {
+        const int rep = tent[t];
+        const uint32_t* e = R.kmer + R.kmer_off[rep];
+        const int ne = R.n_kmer[rep];
+        const uint32_t bit = 1u << (t & 31);
+        int ex = 0;
+        for (int i = lane; i < ne; i += 32) {
+            const uint32_t v = __ldg(e + i);
+            const uint32_t c = v & 0xffffu;
+            if (c) {
+                atomicOr(tmask + (v >> 16) * row_words + (t >> 5), bit);
+                ex += (int)c - 1;
+            }
+        }
+        ex = warp_sum_i(ex);
+        if (lane == 0) tex[t] = ex;
+    }
+}
+
+// p += w0 + .. + w7, bit-sliced (8 planes, counts below 256): a Harley-Seal
+// tree of carry-save adders into the planes of weight 1, 2 and 4, then the
+// carry of weight 8 rippled into the rest.
+__device__ __forceinline__ void bs_add8(uint32_t (&p)[8], uint32_t w0, uint32_t w1, uint32_t w2,
+                                        uint32_t w3, uint32_t w4, uint32_t w5, uint32_t w6,
+                                        uint32_t w7) {
+    uint32_t t1, t2, t3, t4, f1, f2, e8;
+    csa(p[0], t1, p[0], w0, w1);
+    csa(p[0], t2, p[0], w2, w3);
+    csa(p[1], f1, p[1], t1, t2);
+    csa(p[0], t3, p[0], w4, w5);
+    csa(p[0], t4, p[0], w6, w7);
+    csa(p[1], f2, p[1], t3, t4);
+    csa(p[2], e8, p[2], f1, f2);
+#pragma unroll
+    for (int b = 3; b < 8; b++) {
+        const uint32_t c = p[b] & e8;
+        p[b] ^= e8;
+        e8 = c;
+    }
+}
+
+// a += b, bit-sliced (ripple carry over 8 planes).
+__device__ __forceinline__ void bs_add(uint32_t (&a)[8], const uint32_t (&b)[8]) {
+    uint32_t c = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) csa(a[i], c, a[i], b[i], c);
+}
+
+// Bits of the counts >= v.
+__device__ __forceinline__ uint32_t bs_ge(const uint32_t (&p)[8], int v) {
+    if (v <= 0) return 0xffffffffu;
+    if (v > 255) return 0u;
+    uint32_t gt = 0, eq = 0xffffffffu;
+#pragma unroll
+    for (int b = 7; b >= 0; b--) {
+        const uint32_t vb = ((v >> b) & 1) ? 0xffffffffu : 0u;
+        gt |= eq & p[b] & ~vb;
+        eq &= ~(p[b] ^ vb);
+    }
+    return gt | eq;
+}
+
+__device__ __forceinline__ int bs_get(const uint32_t (&p)[8], int bit) {
+    int v = 0;
+#pragma unroll
+    for (int b = 0; b < 8; b++) v |= (int)((p[b] >> bit) & 1u) << b;
+    return v;
+}
+
+struct MaskCounts {
+    unsigned long long n_pf = 0, bytes = 0;
+    unsigned n_wf = 0, n_al = 0;
+};
+
+// The candidates of one warp with LPR lanes per row (LPR x 16 bytes hold the
+// pass's tentatives): the warp's 32 / LPR row groups take every
+// (32 / LPR)-th k-mer, then a butterfly over the groups adds their counts.
+template <int LPR>
+__device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* st,
+                                                const int32_t* __restrict__ remain,
+                                                const int32_t* s_tent, int nt, int n,
+                                                const uint4* __restrict__ tm4, int rwq,
+                                                const int32_t* __restrict__ tex, Pair* pairs,
+                                                int seg_cap, Pair* amb, int amb_cap,
+                                                MaskCounts& mc) {
+    constexpr int RPI = 32 / LPR;  // rows per load instruction
+    constexpr int NV = RPI / 4;    // entry registers per step (8 rows per lane)
+    const int lane = threadIdx.x & 31;
+    const int g = lane / LPR, x = lane % LPR;
+    const bool xin = x < ((nt + 127) >> 7);
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < n; idx += nwarps) {
+        const int q = remain[idx];
+        // tentatives before q: the first ntq of the ascending list
+        int lo = 0, hi = nt;
+        if (s_tent[nt - 1] < q) lo = nt;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (s_tent[mid] < q) lo = mid + 1;
+            else hi = mid;
+        }
+        const int ntq = lo;
+        mc.n_pf += ntq;
+        if (ntq == 0) continue;
+        const uint32_t* e = R.kmer + R.kmer_off[q];
+        const int ne = R.n_kmer[q];
+        mc.bytes += kCandFixedBytes + 4ull * (unsigned)ne;
+        uint32_t P[4][8];
+#pragma unroll
+        for (int s = 0; s < 4; s++)
+#pragma unroll
+            for (int b = 0; b < 8; b++) P[s][b] = 0u;
+        int ex = 0;
+        for (int base = 0; base < ne; base += 8 * RPI) {
+            uint32_t vv[NV];
+#pragma unroll
+            for (int r = 0; r < NV; r++) {
+                const int i = base + 32 * r + lane;
+                vv[r] = i < ne ? __ldcs(e + i) : 0u;
+                const int c = (int)(vv[r] & 0xffffu);
+                ex += c > 0 ? c - 1 : 0;
+            }
+            uint4 w[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int il = u * RPI + g;
+                const uint32_t v = __shfl_sync(kFull, vv[(u * RPI) >> 5], il & 31);
+                w[u] = make_uint4(0u, 0u, 0u, 0u);
+                if (xin && base + il < ne && (v & 0xffffu)) w[u] = __ldg(tm4 + (size_t)(v >> 16) * rwq + x);
+            }
+            bs_add8(P[0], w[0].x, w[1].x, w[2].x, w[3].x, w[4].x, w[5].x, w[6].x, w[7].x);
+            bs_add8(P[1], w[0].y, w[1].y, w[2].y, w[3].y, w[4].y, w[5].y, w[6].y, w[7].y);
+            bs_add8(P[2], w[0].z, w[1].z, w[2].z, w[3].z, w[4].z, w[5].z, w[6].z, w[7].z);
+            bs_add8(P[3], w[0].w, w[1].w, w[2].w, w[3].w, w[4].w, w[5].w, w[6].w, w[7].w);
+        }
+        // every lane ends with the whole counts of its 16 bytes of tentatives
+#pragma unroll
+        for (int off = LPR; off < 32; off <<= 1)
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                uint32_t o[8];
+#pragma unroll
+                for (int b = 0; b < 8; b++) o[b] = __shfl_xor_sync(kFull, P[s][b], off);
+                bs_add(P[s], o);
+            }
+        ex = warp_sum_i(ex);
+        // group g < 4 decides word g of the lane's 16 bytes: tentatives
+        // [32 (4x + g), +32)
+        if (g >= 4 || !xin) continue;
+        uint32_t Pw[8];
+#pragma unroll
+        for (int b = 0; b < 8; b++) Pw[b] = P[0][b];
+#pragma unroll
+        for (int s = 1; s < 4; s++)
+            if (g == s)
+#pragma unroll
+                for (int b = 0; b < 8; b++) Pw[b] = P[s][b];
+        const int t0 = 32 * (4 * x + g);
+        if (t0 >= ntq) continue;
+        const uint32_t valid = ntq - t0 >= 32 ? 0xffffffffu : (1u << (ntq - t0)) - 1u;
+        const int cw = R.cut_word[q];
+        uint32_t pass = bs_ge(Pw, cw) & valid;
+        uint32_t open = bs_ge(Pw, cw - ex) & valid & ~pass;
+        if (!(pass | open)) continue;
+        const int4 cq = R.comp[q];
+        const int cbq = R.cut_base[q] - R.strict;
+        while (pass) {
+            const int t = t0 + __ffs(pass) - 1;
+            pass &= pass - 1;
+            mc.n_wf++;
+            const int rep = s_tent[t];
+            // the composition bound (kernel_preFilter, func.cu:738-754)
+            if (prefilter_pass(R.comp[rep], cq, cbq)) {
+                push_pair(st, pairs, seg_cap, R, rep, q, kBandMaxW);
+                mc.n_al++;
+            }
+        }
+        while (open) {
+            const int b = __ffs(open) - 1;
+            open &= open - 1;
+            const int t = t0 + b;
+            if (bs_get(Pw, b) + min(tex[t], ex) < cw) continue;
+            mc.n_wf++;
+            const int rep = s_tent[t];
+            if (prefilter_pass(R.comp[rep], cq, cbq)) {
+                const int slot = atomicAdd(&st->n_amb, 1);
+                if (slot < amb_cap) amb[slot] = Pair{rep, q};
+                else st->pair_overflow = 1;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kMaskThreads, 2) k_bfilter_mask(
+    DevReads R, RoundState* st, const int32_t* __restrict__ remain,
+    const int32_t* __restrict__ tent, const uint4* __restrict__ tm4, int rwq,
+    const int32_t* __restrict__ tex, Pair* pairs, int seg_cap, Pair* amb, int amb_cap) {
+    __shared__ int32_t s_tent[kMaxBatch];
+    if (st->done || st->n_tent == 0) return;
+    const int nt = st->n_tent;
+    const int n = st->n_remain;
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) s_tent[i] = tent[i];
+    __syncthreads();
+    MaskCounts mc;
+    const int quads = (nt + 127) >> 7;  // 16-byte words of the pass's rows
+    if (quads > 4)
+        mask_candidates<8>(R, st, remain, s_tent, nt, n, tm4, rwq, tex, pairs, seg_cap, amb,
+                           amb_cap, mc);
+    else if (quads > 2)
+        mask_candidates<4>(R, st, remain, s_tent, nt, n, tm4, rwq, tex, pairs, seg_cap, amb,
+                           amb_cap, mc);
+    else if (quads > 1)
+        mask_candidates<2>(R, st, remain, s_tent, nt, n, tm4, rwq, tex, pairs, seg_cap, amb,
+                           amb_cap, mc);
+    else
+        mask_candidates<1>(R, st, remain, s_tent, nt, n, tm4, rwq, tex, pairs, seg_cap, amb,
+                           amb_cap, mc);
+    // n_pf and bytes are the same in every lane; n_wf and n_al are per lane
+    const unsigned n_wf = (unsigned)warp_sum_i((int)mc.n_wf);
+    const unsigned n_al = (unsigned)warp_sum_i((int)mc.n_al);
+    if ((threadIdx.x & 31) == 0) {
+        if (mc.n_pf) atomicAdd(&st->cnt_prefilter, mc.n_pf);
+        if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
+        if (n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
+        if (mc.bytes) atomicAdd(&st->filter_bytes, mc.bytes);
+    }
+}
+
 // Survival of the tentatives in greedy order (one warp): a tentative survives
 // iff no surviving earlier tentative accepted it.  Only rows with a bit can
 // claim anything, so only those are visited, in increasing order.
@@ -2099,6 +2358,26 @@ void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* re
         R, B.st, B.amb, B.amb_cap, B.pairs, B.seg_cap);
 }
 
+template <int K>
+void launch_bfilter_mask_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
+                           cudaStream_t s) {
+    constexpr int xsmem = (kExactThreads<K> / 32) * (1 << (2 * K)) * 2;
+    static int grid = 0, xgrid = 0;
+    if (!grid) {
+        cudaFuncSetAttribute(k_bexact<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, xsmem);
+        grid = grid_for(k_bfilter_mask, kMaskThreads, 0, 2);
+        xgrid = grid_for(k_bexact<K>, kExactThreads<K>, xsmem, 8);
+    }
+    cudaMemsetAsync(B.tmask, 0, sizeof(uint4) * ((size_t)1 << (2 * K)) * B.tmask_rwq, s);
+    k_bmask<<<kMaxBatch / 8, 256, 0, s>>>(R, B.st, B.tent, reinterpret_cast<uint32_t*>(B.tmask),
+                                          B.tmask_ex, B.tmask_rwq);
+    k_bfilter_mask<<<shaped(grid, R.filter_blocks), kMaskThreads, 0, s>>>(
+        R, B.st, remain, B.tent, B.tmask, B.tmask_rwq, B.tmask_ex, B.pairs, B.seg_cap, B.amb,
+        B.amb_cap);
+    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kExactThreads<K>, xsmem, s>>>(
+        R, B.st, B.amb, B.amb_cap, B.pairs, B.seg_cap);
+}
+
 template <bool BATCH>
 void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain, int drop,
                        cudaStream_t s) {
@@ -2108,6 +2387,15 @@ void launch_filter_any(const DevReads& R, RoundBuffers& B, const int32_t* remain
         k_gtab<<<64, 256, 0, s>>>(R, B.st, 0);
         k_filter_g<<<shaped(grid, R.filter_blocks), kFilterThreads, 0, s>>>(R, B.st, remain, B.pairs, B.seg_cap);
         k_gtab<<<64, 256, 0, s>>>(R, B.st, 1);
+        return;
+    }
+    if (BATCH && !drop && B.tmask) {
+        switch (R.k) {
+            case 4: launch_bfilter_mask_t<4>(R, B, remain, s); break;
+            case 5: launch_bfilter_mask_t<5>(R, B, remain, s); break;
+            case 6: launch_bfilter_mask_t<6>(R, B, remain, s); break;
+            default: launch_bfilter_mask_t<7>(R, B, remain, s); break;
+        }
         return;
     }
     if (BATCH && !drop && B.amb) {
@@ -2331,6 +2619,9 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     if (count)
         *count += 8 + align_launches<true>(B) + (!drop ? 1 : 0) +
                   (R.pig_q && !drop ? 1 : 0) + (B.amb && !drop ? 1 : 0);
+    // (a word-filter form launches two kernels, three with the open-pair
+    // queue: the bitmap form k_filter, k_bfilter_bits, k_bexact; the mask
+    // form k_bmask, k_bfilter_mask, k_bexact)
 }
 
 // Whether a job's per-pass k-mer index (at most `cap` postings) is kept in

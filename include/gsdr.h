@@ -50,8 +50,10 @@ typedef struct {
     int32_t stage_timing; /* 1: time each stage with CUDA events (slower; for profiling) */
     int32_t verbose;      /* 1: print the reference's progress lines to stdout */
     int32_t word_filter;  /* batched word filter form: 0 automatic, 1 per-tentative k-mer
-                             tables, 2 inverted k-mer index, 3 k-mer presence bitmaps
-                             (k <= 6); the result is the same in every form */
+                             tables, 2 inverted k-mer index, 3 two-level k-mer count
+                             bitmaps (k <= 7), 4 per-k-mer tentative masks (k <= 7,
+                             reads of at most 255 k-mers; otherwise the automatic
+                             form); the result is the same in every form */
     int32_t variant;      /* semantics: 0 = cuda-version (func.cu, the default);
                              1 = the top-level SYCL program (func.cpp): k from t by
                              func.cpp:36-45, w 4..8, no drop mode and no pigeon filter,
@@ -91,7 +93,8 @@ typedef struct {
     int64_t passes;           /* device passes (batched: one per batch of tentatives) */
     int64_t pairs_prefilter;  /* (representative, candidate) pairs that reached the prefilter */
     int64_t pairs_word;       /* pairs that reached the word filter (word_index = 1: pairs
-                                 that passed it; that form applies the word filter first) */
+                                 that passed it, word_index = 3: pairs its bounds did not
+                                 reject; those forms apply the word filter first) */
     int64_t pairs_aligned;    /* pairs that reached the alignment */
     int64_t pairs_accepted;
     double cells;             /* sum over aligned pairs of gap-free q x T (full-DP cells) */
@@ -107,8 +110,10 @@ typedef struct {
     int64_t kernel_launches;  /* kernels launched by the library during the call */
     int32_t word_index;       /* form of the batched word filter: 0 per-tentative k-mer
                                  tables, 1 per-pass inverted k-mer index (reads holding
-                                 few of the 4^k k-mers), 2 k-mer presence bitmaps with
-                                 an exact sum for the pairs their bound leaves open */
+                                 few of the 4^k k-mers), 2 k-mer count bitmaps with an
+                                 exact sum for the pairs their bound leaves open, 3
+                                 per-k-mer tentative masks (short reads in a sparse
+                                 k-mer space) with the same exact sum */
     double filter_max_bytes;  /* with stage_timing only: input bytes of the filter launch
                                  that read the most, and its time (filter_max_ms) */
     double filter_max_ms;

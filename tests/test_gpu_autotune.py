@@ -86,6 +86,20 @@ def test_word_filter_option_selects_the_form(form):
     np.testing.assert_array_equal(cl, ref)
 
 
+def test_word_filter_option_selects_the_masks():
+    # the mask form takes reads of at most 255 k-mers
+    data = gsdr.synth_fasta(0, n_reads=2000, seed=84, len_lo=60, len_hi=240, n_seeds=300)
+    f = gsdr.Fasta.parse(data)
+    try:
+        cl, st = gsdr.clustering(f, gsdr.default_opts(threshold=0.95, word_filter=4),
+                                 stats=True)
+        ref = gsdr.clustering(f, gsdr.default_opts(threshold=0.95, batch=1))
+    finally:
+        f.close()
+    assert st.word_index == 3
+    np.testing.assert_array_equal(cl, ref)
+
+
 def test_limited_run_stops_early_and_full_run_is_unaffected():
     data = gsdr.synth_fasta(0, n_reads=3000, seed=83)
     f = gsdr.Fasta.parse(data)

@@ -1,9 +1,10 @@
-"""Batched word filter forms against the oracle: the per-pass inverted k-mer
-index (chosen for reads holding few of the 4^k k-mers, e.g. 150 bp reads at
-k = 7), the k-mer presence bitmaps (k <= 6 otherwise) and the per-tentative
-tables.  Identical cluster arrays and FASTA bytes in every form, at every R,
-every word length, and for reads too short to hold a k-mer (the reference's
-kernel_filter, cuda-version/func.cu:803-826)."""
+"""Batched word filter forms against the oracle: the per-k-mer tentative
+masks (chosen for short reads holding few of the 4^k k-mers, e.g. 150 bp
+reads at k = 7), the per-pass inverted k-mer index, the two-level k-mer count
+bitmaps (k <= 7 otherwise) and the per-tentative tables.  Identical cluster
+arrays and FASTA bytes in every form, at every R, every word length, and for
+reads too short to hold a k-mer (the reference's kernel_filter,
+cuda-version/func.cu:803-826)."""
 import numpy as np
 import pytest
 
@@ -33,22 +34,31 @@ def run_form(data, tmp_path, monkeypatch, t, batch, form, w=0, d=3):
 
 
 @pytest.mark.parametrize("batch", [2, 64, 256, 1024, 0])
-def test_c2_recipe_index_auto(tmp_path, monkeypatch, batch):
+def test_c2_recipe_masks_auto(tmp_path, monkeypatch, batch):
     data = gsdr.synth_fasta(2, n_reads=30000, seed=33)
     st, ost = run_form(data, tmp_path, monkeypatch, 0.90, batch, None)
-    assert st.k == 7 and st.word_index == 1
+    assert st.k == 7 and st.word_index == 3
     # the pairs sent to the alignment are the pairs passing both filters
     assert st.passes < st.rounds
 
 
-def test_c2_recipe_same_pairs_both_forms(tmp_path, monkeypatch):
+@pytest.mark.parametrize("batch", [2, 64, 256, 1024])
+def test_c2_recipe_index_forced(tmp_path, monkeypatch, batch):
+    data = gsdr.synth_fasta(2, n_reads=30000, seed=33)
+    st, ost = run_form(data, tmp_path, monkeypatch, 0.90, batch, "index")
+    assert st.k == 7 and st.word_index == 1
+
+
+def test_c2_recipe_same_pairs_every_form(tmp_path, monkeypatch):
     data = gsdr.synth_fasta(2, n_reads=20000, seed=34)
     si, _ = run_form(data, tmp_path, monkeypatch, 0.90, 128, "index")
     stt, _ = run_form(data, tmp_path, monkeypatch, 0.90, 128, "table")
-    assert si.word_index == 1 and stt.word_index == 0
-    assert si.pairs_prefilter == stt.pairs_prefilter
-    assert si.pairs_aligned == stt.pairs_aligned
-    assert si.cells == stt.cells
+    sm, _ = run_form(data, tmp_path, monkeypatch, 0.90, 128, "masks")
+    assert si.word_index == 1 and stt.word_index == 0 and sm.word_index == 3
+    for s in (si, sm):
+        assert s.pairs_prefilter == stt.pairs_prefilter
+        assert s.pairs_aligned == stt.pairs_aligned
+        assert s.cells == stt.cells
 
 
 @pytest.mark.parametrize("t", [0.88, 0.90, 0.93, 0.97])
@@ -71,7 +81,7 @@ def test_index_long_reads(tmp_path, monkeypatch):
     assert st.word_index == 1
 
 
-@pytest.mark.parametrize("form", ["index", "table"])
+@pytest.mark.parametrize("form", ["index", "table", "masks"])
 def test_very_short_reads(tmp_path, monkeypatch, form):
     # 3-48 bp reads at k = 7: reads of at most 6 bases hold no k-mer, and the
     # word cutoff is never below 1 (func.cu:312-337), so they are never aligned
@@ -80,7 +90,7 @@ def test_very_short_reads(tmp_path, monkeypatch, form):
     cw, _, _ = orc.cutoffs(lens, 0.90, 7)
     assert (lens <= 6).any() and (cw >= 1).all()
     st, _ = run_form(data, tmp_path, monkeypatch, 0.90, 64, form, w=7)
-    assert st.word_index == (1 if form == "index" else 0)
+    assert st.word_index == {"index": 1, "table": 0, "masks": 3}[form]
 
 
 def test_index_form_is_repeatable(monkeypatch):
@@ -171,3 +181,92 @@ def test_bits_same_pairs_as_tables(tmp_path, monkeypatch):
     assert sb.pairs_word == stt.pairs_word
     assert sb.pairs_aligned == stt.pairs_aligned
     assert sb.cells == stt.cells
+
+
+# ---- per-k-mer tentative masks: D1 <= S <= D1 + min(excess), bit-sliced
+# counts, exact sums for the pairs the bound leaves open
+
+# R values that take each row width: 1, 2, 4 and 8 lanes per row of
+# 16-byte words, with partly used words (100, 129, 300, 513)
+@pytest.mark.parametrize("batch", [2, 100, 129, 300, 513, 1024])
+def test_masks_row_widths(tmp_path, monkeypatch, batch):
+    data = gsdr.synth_fasta(2, n_reads=12000, seed=46)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.90, batch, "masks")
+    assert st.k == 7 and st.word_index == 3
+
+
+@pytest.mark.parametrize("w", [4, 5, 6, 7])
+def test_masks_word_lengths_ragged_reads(tmp_path, monkeypatch, w):
+    # 20-240 bp seeds (copies with insertions run a few bases longer): below
+    # 256 k-mer entries per read at k = 4
+    data = gsdr.synth_fasta(0, n_reads=2500, seed=47, len_lo=20, len_hi=240, n_seeds=500)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 256, "masks", w=w)
+    assert st.k == w and st.word_index == 3
+
+
+@pytest.mark.parametrize("t", [0.88, 0.90, 0.93, 0.97])
+def test_masks_thresholds(tmp_path, monkeypatch, t):
+    data = gsdr.synth_fasta(0, n_reads=2500, seed=48, len_lo=60, len_hi=240, n_seeds=400)
+    st, ost = run_form(data, tmp_path, monkeypatch, t, 0, "masks")
+    assert st.k == ost.k
+    if st.k <= 7:
+        assert st.word_index == 3
+
+
+def repeat_reads(rng, n_seeds=120, copies=12):
+    """Low-complexity reads (tandem repeats of 1-12 bp units, 80-250 bp) and
+    their copies with a few substitutions and indels: k-mer counts well above
+    one, so the mask bound leaves pairs open for the exact sums."""
+    recs = []
+    for s in range(n_seeds):
+        unit = rng.choice(list(b"ACGT"), size=int(rng.integers(1, 13))).astype(np.uint8)
+        L = int(rng.integers(80, 251))
+        seed = np.resize(unit, L)
+        if s % 3 == 0:  # a random stretch inside the repeat
+            a = int(rng.integers(0, L // 2))
+            seed[a:a + L // 4] = rng.choice(list(b"ACGT"), size=len(seed[a:a + L // 4]))
+        for c in range(copies):
+            r = seed.copy()
+            for _ in range(int(rng.integers(0, 6))):
+                p = int(rng.integers(0, len(r)))
+                op = int(rng.integers(0, 3))
+                if op == 0:
+                    r[p] = rng.choice(list(b"ACGT"))
+                elif op == 1 and len(r) > 40:
+                    r = np.delete(r, p)
+                else:
+                    r = np.insert(r, p, rng.choice(list(b"ACGT")))
+            recs.append(bytes(r[:255]))
+    order = rng.permutation(len(recs))
+    return b"".join(b">r%d\n%s\n" % (i, recs[j]) for i, j in enumerate(order))
+
+
+@pytest.mark.parametrize("t,batch", [(0.90, 64), (0.90, 0), (0.95, 512), (0.88, 1024)])
+def test_masks_low_complexity_open_pairs(tmp_path, monkeypatch, t, batch):
+    data = repeat_reads(np.random.default_rng(49))
+    st, _ = run_form(data, tmp_path, monkeypatch, t, batch, "masks")
+    assert st.word_index == 3
+
+
+def test_masks_fall_back_for_long_reads(tmp_path, monkeypatch):
+    # reads above 255 k-mers: the counts would not fit the masks' 8 planes,
+    # so the forced form falls back to the automatic one
+    data = gsdr.synth_fasta(0, n_reads=1500, seed=50)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 64, "masks")
+    assert st.word_index != 3
+
+
+def test_masks_form_is_repeatable(monkeypatch):
+    monkeypatch.delenv("GSDR_BFILTER", raising=False)
+    data = gsdr.synth_fasta(2, n_reads=20000, seed=39)
+    f = gsdr.Fasta.parse(data)
+    job = gsdr.Job(f, gsdr.default_opts(threshold=0.90, batch=0))
+    try:
+        assert job.run().word_index == 3
+        a = job.cluster()
+        job.run()
+        b = job.cluster()
+    finally:
+        job.close()
+        f.close()
+    assert np.array_equal(a, b)

@@ -181,10 +181,11 @@ def test_block_shape_and_staging_depth_ranges(knobs, ok):
 
 
 def test_word_filter_option_range():
-    o = gsdr.default_opts(word_filter=4)
-    with pytest.raises(gsdr.GsdrError):
-        gsdr.resolve_opts(o)
+    for bad in (5, -1):
+        with pytest.raises(gsdr.GsdrError):
+            gsdr.resolve_opts(gsdr.default_opts(word_filter=bad))
     assert gsdr.resolve_opts(gsdr.default_opts(word_filter=2)).word_filter == 2
+    assert gsdr.resolve_opts(gsdr.default_opts(word_filter=4)).word_filter == 4
 
 
 @pytest.mark.parametrize("kw", [{"group_words": 129}, {"group_words": -2},
