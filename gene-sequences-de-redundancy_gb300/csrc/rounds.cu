@@ -1742,9 +1742,10 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
 //
 // Per pass, for every k-mer m a row of R_max bits, bit t set iff tentative t
 // holds m with a non-zero count (k_bmask; 2 MB for k = 7 and R_max 1024, held
-// in L2).  One warp per candidate loads the rows of the candidate's k-mers, 16
-// bytes per lane, so one load instruction brings four rows of 1,024
-// tentatives, and counts per tentative the rows that have its bit:
+// in L2).  A group of lanes per candidate (eight lanes of 16 bytes hold a row
+// of 1,024 tentatives; four candidates per warp) copies the rows of the
+// candidate's k-mers into shared memory and counts per tentative the rows
+// that have its bit:
 //     D1 = sum over k-mers of [c_t >= 1][c_q >= 1],
 // in bit-sliced counters (plane b holds bit b of 32 tentatives' counts) that
 // carry-save adders fill.  Since min(c_t, c_q) = [both >= 1] + (min - 1),
@@ -1810,13 +1811,6 @@ __device__ __forceinline__ void bs_add8(uint32_t (&p)[8], uint32_t w0, uint32_t 
     }
 }
 
-// a += b, bit-sliced (ripple carry over 8 planes).
-__device__ __forceinline__ void bs_add(uint32_t (&a)[8], const uint32_t (&b)[8]) {
-    uint32_t c = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) csa(a[i], c, a[i], b[i], c);
-}
-
 // Bits of the counts >= v.
 __device__ __forceinline__ uint32_t bs_ge(const uint32_t (&p)[8], int v) {
     if (v <= 0) return 0xffffffffu;
@@ -1843,152 +1837,232 @@ struct MaskCounts {
     unsigned n_wf = 0, n_al = 0;
 };
 
-// The candidates of one warp with LPR lanes per row (LPR x 16 bytes hold the
-// pass's tentatives): the warp's 32 / LPR row groups take every
-// (32 / LPR)-th k-mer, then a butterfly over the groups adds their counts.
+// Rows stream through shared memory with cp.async, kMaskStages steps deep:
+// each lane copies its own 16-byte words and reads back only those, so no
+// warp barrier is needed (the kernel is bound by L2 latency, and the copies
+// in flight hold no registers).
+constexpr int kMaskStages = 3;
+constexpr int kMaskStepBytes = 8 * 32 * 16;  // one step: 8 words of 16 bytes per lane
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool fill) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem),
+                 "r"(fill ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+// Rows of 16-byte words: lane (g, x) of a warp, g = lane / LPR, x = lane %
+// LPR, works for candidate g of the warp's 32 / LPR consecutive candidates
+// (consecutive in the remain list, so of similar length) and holds the counts
+// of word x of the rows (tentatives 128 x .. 128 x + 127).  Each step a group
+// copies the rows of 8 of its candidate's k-mers; the entries of the step
+// after next load one step ahead of their copies, the copies kMaskStages - 1
+// steps ahead of their counts.
 template <int LPR>
 __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* st,
                                                 const int32_t* __restrict__ remain,
-                                                const int32_t* s_tent, int nt, int n,
-                                                const uint4* __restrict__ tm4, int rwq,
+                                                const int32_t* s_tent, uint4* stage, int nt,
+                                                int n, const uint4* __restrict__ tm4, int rwq,
                                                 const int32_t* __restrict__ tex, Pair* pairs,
                                                 int seg_cap, Pair* amb, int amb_cap,
                                                 MaskCounts& mc) {
-    constexpr int RPI = 32 / LPR;  // rows per load instruction
-    constexpr int NV = RPI / 4;    // entry registers per step (8 rows per lane)
+    constexpr int G = 32 / LPR;   // candidates per warp
+    constexpr int EPL = 8 / LPR;  // entries a lane loads per step
     const int lane = threadIdx.x & 31;
     const int g = lane / LPR, x = lane % LPR;
     const bool xin = x < ((nt + 127) >> 7);
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < n; idx += nwarps) {
-        const int q = remain[idx];
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int base = wid * G; base < n; base += nwarps * G) {
+        const int idx = base + g;
+        const int q = idx < n ? remain[idx] : -1;
         // tentatives before q: the first ntq of the ascending list
-        int lo = 0, hi = nt;
-        if (s_tent[nt - 1] < q) lo = nt;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (s_tent[mid] < q) lo = mid + 1;
-            else hi = mid;
+        int ntq = 0;
+        if (q >= 0) {
+            int lo = 0, hi = nt;
+            if (s_tent[nt - 1] < q) lo = nt;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s_tent[mid] < q) lo = mid + 1;
+                else hi = mid;
+            }
+            ntq = lo;
         }
-        const int ntq = lo;
-        mc.n_pf += ntq;
-        if (ntq == 0) continue;
-        const uint32_t* e = R.kmer + R.kmer_off[q];
-        const int ne = R.n_kmer[q];
-        mc.bytes += kCandFixedBytes + 4ull * (unsigned)ne;
-        uint32_t P[4][8];
-#pragma unroll
-        for (int s = 0; s < 4; s++)
-#pragma unroll
-            for (int b = 0; b < 8; b++) P[s][b] = 0u;
+        const int ne = ntq > 0 ? R.n_kmer[q] : 0;
+        const uint32_t* e = R.kmer + (ntq > 0 ? R.kmer_off[q] : 0);
+        if (x == 0) {
+            mc.n_pf += ntq;
+            if (ntq > 0) mc.bytes += kCandFixedBytes + 4ull * (unsigned)ne;
+        }
+        const int nsteps = __reduce_max_sync(kFull, (ne + 7) >> 3);
+        if (nsteps == 0) continue;
+        // entries [8 j + EPL x, + EPL) of the candidate (the lists are padded
+        // to 16 bytes, with slack after the last: whole vectors load)
+        uint32_t en[EPL];
         int ex = 0;
-        for (int base = 0; base < ne; base += 8 * RPI) {
-            uint32_t vv[NV];
+        auto load_entries = [&](int j) {
+            const int i0 = 8 * j + EPL * x;
 #pragma unroll
-            for (int r = 0; r < NV; r++) {
-                const int i = base + 32 * r + lane;
-                vv[r] = i < ne ? __ldcs(e + i) : 0u;
-                const int c = (int)(vv[r] & 0xffffu);
+            for (int k = 0; k < EPL; k++) en[k] = 0u;
+            if (i0 < ne) {
+                if constexpr (EPL == 1) {
+                    en[0] = __ldcs(e + i0);
+                } else if constexpr (EPL == 2) {
+                    const uint2 v = __ldcs(reinterpret_cast<const uint2*>(e + i0));
+                    en[0] = v.x, en[1] = v.y;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < EPL; k += 4) {
+                        const uint4 v = __ldcs(reinterpret_cast<const uint4*>(e + i0 + k));
+                        en[k] = v.x, en[k + 1] = v.y, en[k + 2] = v.z, en[k + 3] = v.w;
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < EPL; k++) {
+                if (i0 + k >= ne) en[k] = 0u;
+                const int c = (int)(en[k] & 0xffffu);
                 ex += c > 0 ? c - 1 : 0;
             }
-            uint4 w[8];
+        };
+        // step j: slot u of stage j % kMaskStages gets word x of the row of
+        // entry 8 j + u
+        auto issue = [&](int j) {
+            uint4* dst = stage + (j % kMaskStages) * (kMaskStepBytes / 16) + lane;
 #pragma unroll
             for (int u = 0; u < 8; u++) {
-                const int il = u * RPI + g;
-                const uint32_t v = __shfl_sync(kFull, vv[(u * RPI) >> 5], il & 31);
-                w[u] = make_uint4(0u, 0u, 0u, 0u);
-                if (xin && base + il < ne && (v & 0xffffu)) w[u] = __ldg(tm4 + (size_t)(v >> 16) * rwq + x);
+                const uint32_t v = EPL == 8 ? en[u % EPL]
+                                            : __shfl_sync(kFull, en[u % EPL], g * LPR + u / EPL);
+                const bool ok = xin && (v & 0xffffu);
+                cp_async16(dst + 32 * u, ok ? tm4 + (size_t)(v >> 16) * rwq + x : tm4, ok);
             }
+        };
+        uint32_t P[4][8];
+#pragma unroll
+        for (int w = 0; w < 4; w++)
+#pragma unroll
+            for (int b = 0; b < 8; b++) P[w][b] = 0u;
+        load_entries(0);
+#pragma unroll
+        for (int j = 0; j < kMaskStages - 1; j++) {
+            if (j < nsteps) {
+                issue(j);
+                load_entries(j + 1);
+            }
+            cp_async_commit();
+        }
+        for (int s = 0; s < nsteps; s++) {
+            const int j = s + kMaskStages - 1;
+            if (j < nsteps) {
+                issue(j);
+                load_entries(j + 1);
+            }
+            cp_async_commit();
+            cp_async_wait<kMaskStages - 1>();  // this lane's copies of step s
+            const uint4* src = stage + (s % kMaskStages) * (kMaskStepBytes / 16) + lane;
+            uint4 w[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) w[u] = src[32 * u];
             bs_add8(P[0], w[0].x, w[1].x, w[2].x, w[3].x, w[4].x, w[5].x, w[6].x, w[7].x);
             bs_add8(P[1], w[0].y, w[1].y, w[2].y, w[3].y, w[4].y, w[5].y, w[6].y, w[7].y);
             bs_add8(P[2], w[0].z, w[1].z, w[2].z, w[3].z, w[4].z, w[5].z, w[6].z, w[7].z);
             bs_add8(P[3], w[0].w, w[1].w, w[2].w, w[3].w, w[4].w, w[5].w, w[6].w, w[7].w);
         }
-        // every lane ends with the whole counts of its 16 bytes of tentatives
+        // E_q over the group's lanes
 #pragma unroll
-        for (int off = LPR; off < 32; off <<= 1)
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                uint32_t o[8];
-#pragma unroll
-                for (int b = 0; b < 8; b++) o[b] = __shfl_xor_sync(kFull, P[s][b], off);
-                bs_add(P[s], o);
-            }
-        ex = warp_sum_i(ex);
-        // group g < 4 decides word g of the lane's 16 bytes: tentatives
-        // [32 (4x + g), +32)
-        if (g >= 4 || !xin) continue;
-        uint32_t Pw[8];
-#pragma unroll
-        for (int b = 0; b < 8; b++) Pw[b] = P[0][b];
-#pragma unroll
-        for (int s = 1; s < 4; s++)
-            if (g == s)
-#pragma unroll
-                for (int b = 0; b < 8; b++) Pw[b] = P[s][b];
-        const int t0 = 32 * (4 * x + g);
-        if (t0 >= ntq) continue;
-        const uint32_t valid = ntq - t0 >= 32 ? 0xffffffffu : (1u << (ntq - t0)) - 1u;
+        for (int off = 1; off < LPR; off <<= 1) ex += __shfl_xor_sync(kFull, ex, off);
+        if (ntq == 0 || !xin) continue;
         const int cw = R.cut_word[q];
-        uint32_t pass = bs_ge(Pw, cw) & valid;
-        uint32_t open = bs_ge(Pw, cw - ex) & valid & ~pass;
-        if (!(pass | open)) continue;
-        const int4 cq = R.comp[q];
-        const int cbq = R.cut_base[q] - R.strict;
-        while (pass) {
-            const int t = t0 + __ffs(pass) - 1;
-            pass &= pass - 1;
-            mc.n_wf++;
-            const int rep = s_tent[t];
-            // the composition bound (kernel_preFilter, func.cu:738-754)
-            if (prefilter_pass(R.comp[rep], cq, cbq)) {
-                push_pair(st, pairs, seg_cap, R, rep, q, kBandMaxW);
-                mc.n_al++;
+        // counts >= v need a bit at or above plane floor(log2 v): most words
+        // have none and skip the comparisons
+        const int vlo = cw - ex;
+        const int lb = vlo > 0 ? 31 - __clz(vlo) : 0;
+        int4 cq = make_int4(0, 0, 0, 0);
+        int cbq = 0;
+        bool have_cq = false;
+#pragma unroll
+        for (int w = 0; w < 4; w++) {
+            const int t0 = 32 * (4 * x + w);
+            if (t0 >= ntq) break;
+            const uint32_t valid = ntq - t0 >= 32 ? 0xffffffffu : (1u << (ntq - t0)) - 1u;
+            uint32_t hiw = 0u;
+#pragma unroll
+            for (int b = 0; b < 8; b++)
+                if (b >= lb) hiw |= P[w][b];
+            if (vlo > 255 || !((vlo <= 0 ? 0xffffffffu : hiw) & valid)) continue;
+            uint32_t pass = bs_ge(P[w], cw) & valid;
+            uint32_t open = bs_ge(P[w], vlo) & valid & ~pass;
+            if (!(pass | open)) continue;
+            if (!have_cq) {
+                cq = R.comp[q];
+                cbq = R.cut_base[q] - R.strict;
+                have_cq = true;
             }
-        }
-        while (open) {
-            const int b = __ffs(open) - 1;
-            open &= open - 1;
-            const int t = t0 + b;
-            if (bs_get(Pw, b) + min(tex[t], ex) < cw) continue;
-            mc.n_wf++;
-            const int rep = s_tent[t];
-            if (prefilter_pass(R.comp[rep], cq, cbq)) {
-                const int slot = atomicAdd(&st->n_amb, 1);
-                if (slot < amb_cap) amb[slot] = Pair{rep, q};
-                else st->pair_overflow = 1;
+            while (pass) {
+                const int t = t0 + __ffs(pass) - 1;
+                pass &= pass - 1;
+                mc.n_wf++;
+                const int rep = s_tent[t];
+                // the composition bound (kernel_preFilter, func.cu:738-754)
+                if (prefilter_pass(R.comp[rep], cq, cbq)) {
+                    push_pair(st, pairs, seg_cap, R, rep, q, kBandMaxW);
+                    mc.n_al++;
+                }
+            }
+            while (open) {
+                const int b = __ffs(open) - 1;
+                open &= open - 1;
+                const int t = t0 + b;
+                if (bs_get(P[w], b) + min(tex[t], ex) < cw) continue;
+                mc.n_wf++;
+                const int rep = s_tent[t];
+                if (prefilter_pass(R.comp[rep], cq, cbq)) {
+                    const int slot = atomicAdd(&st->n_amb, 1);
+                    if (slot < amb_cap) amb[slot] = Pair{rep, q};
+                    else st->pair_overflow = 1;
+                }
             }
         }
     }
+    cp_async_wait<0>();
 }
+
+constexpr int kMaskSmem = (kMaskThreads / 32) * kMaskStages * kMaskStepBytes;
 
 __global__ void __launch_bounds__(kMaskThreads, 2) k_bfilter_mask(
     DevReads R, RoundState* st, const int32_t* __restrict__ remain,
     const int32_t* __restrict__ tent, const uint4* __restrict__ tm4, int rwq,
     const int32_t* __restrict__ tex, Pair* pairs, int seg_cap, Pair* amb, int amb_cap) {
     __shared__ int32_t s_tent[kMaxBatch];
+    extern __shared__ __align__(16) uint4 mstage[];
     if (st->done || st->n_tent == 0) return;
     const int nt = st->n_tent;
     const int n = st->n_remain;
     for (int i = threadIdx.x; i < nt; i += blockDim.x) s_tent[i] = tent[i];
     __syncthreads();
+    uint4* stage = mstage + (threadIdx.x >> 5) * kMaskStages * (kMaskStepBytes / 16);
     MaskCounts mc;
     const int quads = (nt + 127) >> 7;  // 16-byte words of the pass's rows
     if (quads > 4)
-        mask_candidates<8>(R, st, remain, s_tent, nt, n, tm4, rwq, tex, pairs, seg_cap, amb,
-                           amb_cap, mc);
+        mask_candidates<8>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
+                           amb, amb_cap, mc);
     else if (quads > 2)
-        mask_candidates<4>(R, st, remain, s_tent, nt, n, tm4, rwq, tex, pairs, seg_cap, amb,
-                           amb_cap, mc);
+        mask_candidates<4>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
+                           amb, amb_cap, mc);
     else if (quads > 1)
-        mask_candidates<2>(R, st, remain, s_tent, nt, n, tm4, rwq, tex, pairs, seg_cap, amb,
-                           amb_cap, mc);
+        mask_candidates<2>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
+                           amb, amb_cap, mc);
     else
-        mask_candidates<1>(R, st, remain, s_tent, nt, n, tm4, rwq, tex, pairs, seg_cap, amb,
-                           amb_cap, mc);
-    // n_pf and bytes are the same in every lane; n_wf and n_al are per lane
+        mask_candidates<1>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
+                           amb, amb_cap, mc);
     const unsigned n_wf = (unsigned)warp_sum_i((int)mc.n_wf);
     const unsigned n_al = (unsigned)warp_sum_i((int)mc.n_al);
+    mc.n_pf = warp_sum_ull(mc.n_pf);
+    mc.bytes = warp_sum_ull(mc.bytes);
     if ((threadIdx.x & 31) == 0) {
         if (mc.n_pf) atomicAdd(&st->cnt_prefilter, mc.n_pf);
         if (n_wf) atomicAdd(&st->cnt_word, (unsigned long long)n_wf);
@@ -2365,13 +2439,15 @@ void launch_bfilter_mask_t(const DevReads& R, RoundBuffers& B, const int32_t* re
     static int grid = 0, xgrid = 0;
     if (!grid) {
         cudaFuncSetAttribute(k_bexact<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, xsmem);
-        grid = grid_for(k_bfilter_mask, kMaskThreads, 0, 2);
+        cudaFuncSetAttribute(k_bfilter_mask, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kMaskSmem);
+        grid = grid_for(k_bfilter_mask, kMaskThreads, kMaskSmem, 2);
         xgrid = grid_for(k_bexact<K>, kExactThreads<K>, xsmem, 8);
     }
     cudaMemsetAsync(B.tmask, 0, sizeof(uint4) * ((size_t)1 << (2 * K)) * B.tmask_rwq, s);
     k_bmask<<<kMaxBatch / 8, 256, 0, s>>>(R, B.st, B.tent, reinterpret_cast<uint32_t*>(B.tmask),
                                           B.tmask_ex, B.tmask_rwq);
-    k_bfilter_mask<<<shaped(grid, R.filter_blocks), kMaskThreads, 0, s>>>(
+    k_bfilter_mask<<<shaped(grid, R.filter_blocks), kMaskThreads, kMaskSmem, s>>>(
         R, B.st, remain, B.tent, B.tmask, B.tmask_rwq, B.tmask_ex, B.pairs, B.seg_cap, B.amb,
         B.amb_cap);
     k_bexact<K><<<shaped(xgrid, R.filter_blocks), kExactThreads<K>, xsmem, s>>>(
