@@ -1789,12 +1789,14 @@ __global__ void __launch_bounds__(256) k_bmask(DevReads R, RoundState* st,
     }
 }
 
-// p += w0 + .. + w7, bit-sliced (8 planes, counts below 256): a Harley-Seal
-// tree of carry-save adders into the planes of weight 1, 2 and 4, then the
-// carry of weight 8 rippled into the rest.
-__device__ __forceinline__ void bs_add8(uint32_t (&p)[8], uint32_t w0, uint32_t w1, uint32_t w2,
-                                        uint32_t w3, uint32_t w4, uint32_t w5, uint32_t w6,
-                                        uint32_t w7) {
+// p += w0 + .. + w7, bit-sliced (8 planes, counts below 256), in two parts:
+// a Harley-Seal tree of carry-save adders into the planes of weight 1, 2 and
+// 4 that returns the carry of weight 8, and bs_carry, which adds a carry
+// into the planes from `from` up.  Two trees' carries meet in one more adder
+// first (bs_pair8), so the ripple runs once per 16 words.
+__device__ __forceinline__ uint32_t bs_tree8(uint32_t (&p)[8], uint32_t w0, uint32_t w1,
+                                             uint32_t w2, uint32_t w3, uint32_t w4, uint32_t w5,
+                                             uint32_t w6, uint32_t w7) {
     uint32_t t1, t2, t3, t4, f1, f2, e8;
     csa(p[0], t1, p[0], w0, w1);
     csa(p[0], t2, p[0], w2, w3);
@@ -1803,12 +1805,22 @@ __device__ __forceinline__ void bs_add8(uint32_t (&p)[8], uint32_t w0, uint32_t 
     csa(p[0], t4, p[0], w6, w7);
     csa(p[1], f2, p[1], t3, t4);
     csa(p[2], e8, p[2], f1, f2);
+    return e8;
+}
+__device__ __forceinline__ void bs_carry(uint32_t (&p)[8], int from, uint32_t c) {
 #pragma unroll
-    for (int b = 3; b < 8; b++) {
-        const uint32_t c = p[b] & e8;
-        p[b] ^= e8;
-        e8 = c;
+    for (int b = 0; b < 8; b++) {
+        if (b < from) continue;
+        const uint32_t t = p[b] & c;
+        p[b] ^= c;
+        c = t;
     }
+}
+// Two weight-8 carries: one adder into plane 3, its weight-16 carry rippled.
+__device__ __forceinline__ void bs_pair8(uint32_t (&p)[8], uint32_t a8, uint32_t b8) {
+    uint32_t c16;
+    csa(p[3], c16, p[3], a8, b8);
+    bs_carry(p, 4, c16);
 }
 
 // Bits of the counts >= v.
@@ -1901,11 +1913,14 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
         const int nsteps = __reduce_max_sync(kFull, (ne + 7) >> 3);
         if (nsteps == 0) continue;
         // entries [8 j + EPL x, + EPL) of the candidate (the lists are padded
-        // to 16 bytes, with slack after the last: whole vectors load)
-        uint32_t en[EPL];
+        // to 16 bytes, with slack after the last: whole vectors load), kept
+        // as the 16-byte index of their row (-1: no row, count 0 or past the
+        // list)
+        int rb[EPL];
         int ex = 0;
         auto load_entries = [&](int j) {
             const int i0 = 8 * j + EPL * x;
+            uint32_t en[EPL];
 #pragma unroll
             for (int k = 0; k < EPL; k++) en[k] = 0u;
             if (i0 < ne) {
@@ -1924,53 +1939,71 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
             }
 #pragma unroll
             for (int k = 0; k < EPL; k++) {
-                if (i0 + k >= ne) en[k] = 0u;
-                const int c = (int)(en[k] & 0xffffu);
+                const int c = i0 + k < ne ? (int)(en[k] & 0xffffu) : 0;
                 ex += c > 0 ? c - 1 : 0;
+                rb[k] = c > 0 ? (int)(en[k] >> 16) * rwq : -1;
             }
         };
-        // step j: slot u of stage j % kMaskStages gets word x of the row of
-        // entry 8 j + u
-        auto issue = [&](int j) {
-            uint4* dst = stage + (j % kMaskStages) * (kMaskStepBytes / 16) + lane;
+        // stage buffers in turn: copies of step j go to `wr`, counts of step
+        // s read `rd`
+        uint4* const st0 = stage + lane;
+        constexpr int SB = kMaskStepBytes / 16;
+        int wr = 0, rd = 0;
+        // step j: slot u of stage wr gets word x of the row of entry 8 j + u
+        auto issue = [&]() {
+            uint4* dst = st0 + wr * SB;
 #pragma unroll
             for (int u = 0; u < 8; u++) {
-                const uint32_t v = EPL == 8 ? en[u % EPL]
-                                            : __shfl_sync(kFull, en[u % EPL], g * LPR + u / EPL);
-                const bool ok = xin && (v & 0xffffu);
-                cp_async16(dst + 32 * u, ok ? tm4 + (size_t)(v >> 16) * rwq + x : tm4, ok);
+                const int r = EPL == 8 ? rb[u % EPL]
+                                       : __shfl_sync(kFull, rb[u % EPL], g * LPR + u / EPL);
+                const bool ok = xin && r >= 0;
+                cp_async16(dst + 32 * u, tm4 + (ok ? r + x : 0), ok);
             }
+            wr = wr == kMaskStages - 1 ? 0 : wr + 1;
         };
         uint32_t P[4][8];
 #pragma unroll
         for (int w = 0; w < 4; w++)
 #pragma unroll
             for (int b = 0; b < 8; b++) P[w][b] = 0u;
+        uint32_t c8[4] = {0u, 0u, 0u, 0u};  // weight-8 carries of an odd step
         load_entries(0);
 #pragma unroll
         for (int j = 0; j < kMaskStages - 1; j++) {
             if (j < nsteps) {
-                issue(j);
+                issue();
                 load_entries(j + 1);
             }
             cp_async_commit();
         }
         for (int s = 0; s < nsteps; s++) {
-            const int j = s + kMaskStages - 1;
-            if (j < nsteps) {
-                issue(j);
-                load_entries(j + 1);
+            if (s + kMaskStages - 1 < nsteps) {
+                issue();
+                load_entries(s + kMaskStages);
             }
             cp_async_commit();
             cp_async_wait<kMaskStages - 1>();  // this lane's copies of step s
-            const uint4* src = stage + (s % kMaskStages) * (kMaskStepBytes / 16) + lane;
+            const uint4* src = st0 + rd * SB;
+            rd = rd == kMaskStages - 1 ? 0 : rd + 1;
             uint4 w[8];
 #pragma unroll
             for (int u = 0; u < 8; u++) w[u] = src[32 * u];
-            bs_add8(P[0], w[0].x, w[1].x, w[2].x, w[3].x, w[4].x, w[5].x, w[6].x, w[7].x);
-            bs_add8(P[1], w[0].y, w[1].y, w[2].y, w[3].y, w[4].y, w[5].y, w[6].y, w[7].y);
-            bs_add8(P[2], w[0].z, w[1].z, w[2].z, w[3].z, w[4].z, w[5].z, w[6].z, w[7].z);
-            bs_add8(P[3], w[0].w, w[1].w, w[2].w, w[3].w, w[4].w, w[5].w, w[6].w, w[7].w);
+            const uint32_t e0 = bs_tree8(P[0], w[0].x, w[1].x, w[2].x, w[3].x, w[4].x, w[5].x, w[6].x, w[7].x);
+            const uint32_t e1 = bs_tree8(P[1], w[0].y, w[1].y, w[2].y, w[3].y, w[4].y, w[5].y, w[6].y, w[7].y);
+            const uint32_t e2 = bs_tree8(P[2], w[0].z, w[1].z, w[2].z, w[3].z, w[4].z, w[5].z, w[6].z, w[7].z);
+            const uint32_t e3 = bs_tree8(P[3], w[0].w, w[1].w, w[2].w, w[3].w, w[4].w, w[5].w, w[6].w, w[7].w);
+            if (s & 1) {
+                bs_pair8(P[0], c8[0], e0);
+                bs_pair8(P[1], c8[1], e1);
+                bs_pair8(P[2], c8[2], e2);
+                bs_pair8(P[3], c8[3], e3);
+            } else {
+                c8[0] = e0, c8[1] = e1, c8[2] = e2, c8[3] = e3;
+            }
+        }
+        if (nsteps & 1) {
+#pragma unroll
+            for (int w = 0; w < 4; w++) bs_carry(P[w], 3, c8[w]);
         }
         // E_q over the group's lanes
 #pragma unroll
