@@ -1889,9 +1889,21 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
     const bool xin = x < ((nt + 127) >> 7);
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    for (int base = wid * G; base < n; base += nwarps * G) {
-        const int idx = base + g;
-        const int q = idx < n ? remain[idx] : -1;
+    const int stride = nwarps * G;
+    // software pipeline over the warp's candidate sets: the read index of the
+    // set after next and the list position of the next load while this set
+    // is counted
+    auto read_at = [&](int i) { return i < n ? remain[i] : -1; };
+    int q1 = read_at(wid * G + g);
+    int q2 = read_at(wid * G + stride + g);
+    int64_t off1 = q1 >= 0 ? R.kmer_off[q1] : 0;
+    int nk1 = q1 >= 0 ? R.n_kmer[q1] : 0;
+    for (int base = wid * G; base < n; base += stride) {
+        const int q = q1;
+        const int64_t off = off1;
+        const int nk = nk1;
+        q1 = q2;
+        q2 = read_at(base + 2 * stride + g);
         // tentatives before q: the first ntq of the ascending list
         int ntq = 0;
         if (q >= 0) {
@@ -1904,14 +1916,18 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
             }
             ntq = lo;
         }
-        const int ne = ntq > 0 ? R.n_kmer[q] : 0;
-        const uint32_t* e = R.kmer + (ntq > 0 ? R.kmer_off[q] : 0);
+        const int ne = ntq > 0 ? nk : 0;
+        const uint32_t* e = R.kmer + (ntq > 0 ? off : 0);
         if (x == 0) {
             mc.n_pf += ntq;
             if (ntq > 0) mc.bytes += kCandFixedBytes + 4ull * (unsigned)ne;
         }
         const int nsteps = __reduce_max_sync(kFull, (ne + 7) >> 3);
-        if (nsteps == 0) continue;
+        if (nsteps == 0) {
+            off1 = q1 >= 0 ? R.kmer_off[q1] : 0;
+            nk1 = q1 >= 0 ? R.n_kmer[q1] : 0;
+            continue;
+        }
         // entries [8 j + EPL x, + EPL) of the candidate (the lists are padded
         // to 16 bytes, with slack after the last: whole vectors load), kept
         // as the 16-byte index of their row (-1: no row, count 0 or past the
@@ -1976,6 +1992,8 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
             }
             cp_async_commit();
         }
+        off1 = q1 >= 0 ? R.kmer_off[q1] : 0;
+        nk1 = q1 >= 0 ? R.n_kmer[q1] : 0;
         for (int s = 0; s < nsteps; s++) {
             if (s + kMaskStages - 1 < nsteps) {
                 issue();
