@@ -218,6 +218,13 @@ def measured_filter_bound(form, figures):
                 "ipc_of_4": figures.get("c1.filter_bits.ipc"),
                 "dram_pct_of_peak": figures.get("c1.filter_bits.dram_pct"),
                 "source": "profiles/k_bfilter_bits_c1.md (200k-read workload)"}
+    if form == "masks" and figures.get("c2.filter_masks.ipc") is not None:
+        return {"resource": "ALU pipe and L2 latency", "kernel": "k_bfilter_mask",
+                "ipc_of_4": figures["c2.filter_masks.ipc"],
+                "alu_pipe_pct": figures.get("c2.filter_masks.alu_pipe_pct"),
+                "l2_pct_of_peak": figures.get("c2.filter_masks.l2_pct"),
+                "dram_pct_of_peak": figures.get("c2.filter_masks.dram_pct"),
+                "source": "profiles/k_bfilter_mask_c2_300k.md (2M-read workload slice)"}
     if form == "index" and figures.get("c2.filter_index.ipc") is not None:
         return {"resource": "instruction issue", "kernel": "k_bfilter_idx<7>",
                 "ipc_of_4": figures["c2.filter_index.ipc"],

@@ -259,6 +259,12 @@ int autotune(const gsdr_reads* reads, const gsdr_opts* base_in, int reps, int ru
     if (runs <= 0) runs = 2;
     if (reps <= 0) reps = std::max(256, std::min(8192, reads->n / 20));
     const bool drop = base.drop == 1;
+    // the mask form takes reads of at most kMaskMaxEntries k-mer entries: for
+    // longer reads its trials would repeat the automatic form
+    int64_t longest = 0;
+    for (int i = 0; i < reads->n; i++) longest = std::max<int64_t>(longest, reads->length[i]);
+    const bool masks_ok = base.word_length <= kMaxBits2K &&
+                          longest - base.word_length + 1 <= kMaskMaxEntries;
     std::vector<Trial> trials;
     auto best_of = [&]() -> const Trial* {
         const Trial* b = nullptr;
@@ -284,7 +290,7 @@ int autotune(const gsdr_reads* reads, const gsdr_opts* base_in, int reps, int ru
         o.word_filter = 0;
         run(o, "R x form");
         const int rs[] = {64, 256, 1024};
-        for (int form = drop ? 0 : 1; form <= (drop ? 0 : 4); form++)
+        for (int form = drop ? 0 : 1; form <= (drop ? 0 : masks_ok ? 4 : 3); form++)
             for (int r : rs) {
                 o.batch = r;
                 o.word_filter = form;
