@@ -1929,14 +1929,10 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
             continue;
         }
         // entries [8 j + EPL x, + EPL) of the candidate (the lists are padded
-        // to 16 bytes, with slack after the last: whole vectors load), kept
-        // as the 16-byte index of their row (-1: no row, count 0 or past the
-        // list)
-        int rb[EPL];
-        int ex = 0;
-        auto load_entries = [&](int j) {
+        // to 16 bytes, with slack after the last: whole vectors load).  They
+        // stream from HBM, so they load two issues ahead of their copies.
+        auto load_raw = [&](int j, uint32_t (&en)[EPL]) {
             const int i0 = 8 * j + EPL * x;
-            uint32_t en[EPL];
 #pragma unroll
             for (int k = 0; k < EPL; k++) en[k] = 0u;
             if (i0 < ne) {
@@ -1953,20 +1949,23 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
                     }
                 }
             }
-#pragma unroll
-            for (int k = 0; k < EPL; k++) {
-                const int c = i0 + k < ne ? (int)(en[k] & 0xffffu) : 0;
-                ex += c > 0 ? c - 1 : 0;
-                rb[k] = c > 0 ? (int)(en[k] >> 16) * rwq : -1;
-            }
         };
+        int ex = 0;
         // stage buffers in turn: copies of step j go to `wr`, counts of step
         // s read `rd`
         uint4* const st0 = stage + lane;
         constexpr int SB = kMaskStepBytes / 16;
         int wr = 0, rd = 0;
         // step j: slot u of stage wr gets word x of the row of entry 8 j + u
-        auto issue = [&]() {
+        // (a row index of -1: no row, count 0 or past the list)
+        auto issue = [&](int j, const uint32_t (&en)[EPL]) {
+            int rb[EPL];
+#pragma unroll
+            for (int k = 0; k < EPL; k++) {
+                const int c = 8 * j + EPL * x + k < ne ? (int)(en[k] & 0xffffu) : 0;
+                ex += c > 0 ? c - 1 : 0;
+                rb[k] = c > 0 ? (int)(en[k] >> 16) * rwq : -1;
+            }
             uint4* dst = st0 + wr * SB;
 #pragma unroll
             for (int u = 0; u < 8; u++) {
@@ -1983,22 +1982,26 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
 #pragma unroll
             for (int b = 0; b < 8; b++) P[w][b] = 0u;
         uint32_t c8[4] = {0u, 0u, 0u, 0u};  // weight-8 carries of an odd step
-        load_entries(0);
+        uint32_t en0[EPL], en1[EPL];        // entries of the next two steps to issue
+        load_raw(0, en0);
+        load_raw(1, en1);
+        int nexti = 0;  // next step to issue
+        auto issue_next = [&]() {
+            issue(nexti, en0);
+#pragma unroll
+            for (int k = 0; k < EPL; k++) en0[k] = en1[k];
+            load_raw(nexti + 2, en1);
+            nexti++;
+        };
 #pragma unroll
         for (int j = 0; j < kMaskStages - 1; j++) {
-            if (j < nsteps) {
-                issue();
-                load_entries(j + 1);
-            }
+            if (j < nsteps) issue_next();
             cp_async_commit();
         }
         off1 = q1 >= 0 ? R.kmer_off[q1] : 0;
         nk1 = q1 >= 0 ? R.n_kmer[q1] : 0;
         for (int s = 0; s < nsteps; s++) {
-            if (s + kMaskStages - 1 < nsteps) {
-                issue();
-                load_entries(s + kMaskStages);
-            }
+            if (s + kMaskStages - 1 < nsteps) issue_next();
             cp_async_commit();
             cp_async_wait<kMaskStages - 1>();  // this lane's copies of step s
             const uint4* src = st0 + rd * SB;
