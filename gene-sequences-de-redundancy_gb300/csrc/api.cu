@@ -87,10 +87,11 @@ int job_r_max(const gsdr_opts& o) {
     return o.batch == 0 ? 256 : (o.batch > kMaxBatch ? kMaxBatch : (o.batch < 1 ? 1 : o.batch));
 }
 
-// The batched word filter walks an inverted index of the tentatives' k-mers
-// when the reads hold few of the 4^k k-mers (mean distinct k-mers per read at
-// most 4^k / kIndexDensity): then almost every table lookup of the table form
-// would read a zero.  GSDR_BFILTER=index or =table forces either form.
+// Sparse k-mer spaces (mean distinct k-mers per read at most 4^k /
+// kIndexDensity), where almost every table lookup of the table form would
+// read a zero, take the tentative masks when every read has at most
+// kMaskMaxEntries k-mer entries, else the inverted index of the tentatives'
+// k-mers.  GSDR_BFILTER=table|index|bits|masks forces a form.
 constexpr int64_t kIndexDensity = 8;
 
 int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
@@ -525,10 +526,10 @@ int Job::loop_timed() {
                 std::fprintf(stderr,
                              "gsdr trace: step %lld rounds %lld tentatives %d R %d remain %d "
                              "aligned %llu filter %.3f ms align %.3f ms filter_bytes %llu "
-                             "queues%s\n",
+                             "open %d queues%s\n",
                              (long long)h.passes, (long long)h.rounds, h.n_tent, h.R, h.n_remain,
                              (unsigned long long)h.cnt_aligned, a, b,
-                             (unsigned long long)h.filter_bytes, q.c_str());
+                             (unsigned long long)h.filter_bytes, h.n_amb, q.c_str());
             }
         }
         parity ^= 1;

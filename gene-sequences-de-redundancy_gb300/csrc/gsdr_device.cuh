@@ -142,7 +142,7 @@ struct RoundState {
     int32_t acc_overflow;
     int32_t survivors;  // representatives confirmed this pass
     int32_t absorbed;   // reads absorbed this pass
-    int32_t n_amb;      // pairs the bitmap bound left to the exact word filter
+    int32_t n_amb;      // pairs the bitmap or mask bound left to the exact word filter
     int32_t n_pig;      // pairs queued for the pigeon filter
     int32_t pass_limit; // > 0: stop after this many passes (timing runs; result unfinished)
     long long rounds;   // representatives taken so far
