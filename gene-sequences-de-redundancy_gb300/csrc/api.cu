@@ -244,6 +244,8 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     // (four alignment queues' worth: a pass whose open pairs overflow it is redone)
     B.amb_cap = P.bits || P.masks ? 4 * B.seg_cap : 0;
     B.amb = P.bits || P.masks ? c.take<Pair>((size_t)B.amb_cap) : nullptr;
+    B.amb2 = P.bits || P.masks ? c.take<Pair>((size_t)B.amb_cap) : nullptr;
+    B.amb_idx = P.bits || P.masks ? c.take<int32_t>(4 * (size_t)(kMaxBatch + 1)) : nullptr;
     B.tmask_rwq = P.masks ? (P.r_max + 127) / 128 : 0;
     B.tmask = P.masks ? c.take<uint4>(((size_t)1 << (2 * k)) * B.tmask_rwq) : nullptr;
     B.tmask_ex = P.masks ? c.take<int32_t>(kMaxBatch) : nullptr;

@@ -208,6 +208,9 @@ struct RoundBuffers {
     // cannot decide
     Pair* amb;           // amb_cap pairs
     int32_t amb_cap;
+    Pair* amb2;          // the same pairs grouped by tentative (amb_cap)
+    int32_t* amb_idx;    // 4 x (kMaxBatch + 1): per tentative counts (zero between
+                         // passes), run offsets, cursors, work items
     // batched word filter by tentative masks (short reads, k <= 7; null =
     // another form): row m (tmask_rwq x 16 bytes) has bit t set iff tentative
     // t holds k-mer m; tmask_ex[t] = its excess, sum of (count - 1).  Zeroed

@@ -25,10 +25,12 @@
 // joins the first surviving tentative that accepted it.  That is exactly what
 // R consecutive reference rounds produce.
 //   k_bselect     next R unclustered indices from a forward cursor
-//   k_bfilter_tab / k_bfilter_idx / k_bfilter_bits (+ k_bexact)
+//   k_bfilter_tab / k_bfilter_idx / k_bfilter_bits / k_bfilter_mask (+ k_bexact_t)
 //                 prefilter + word filter of (tentative group, candidate):
-//                 transposed per-tentative tables, an inverted k-mer index, or
-//                 k-mer presence bitmaps; k_bprefilter in drop mode
+//                 transposed per-tentative tables, an inverted k-mer index,
+//                 k-mer count bitmaps or per-k-mer tentative masks (the last
+//                 two with exact sums for the pairs their bounds leave open);
+//                 k_bprefilter in drop mode
 //   k_align       as above, accepted pairs listed instead of applied
 //   k_bsurvive    survival of the tentatives in order (one warp)
 //   k_bclaim      first surviving tentative per candidate (keyed atomicMax)
@@ -1231,7 +1233,7 @@ __global__ void __launch_bounds__(kFilterThreads) k_bprefilter(DevReads R, Round
 // with D1, D2 the popcounts of the two levels' intersections.  k_bfilter_bits
 // forms lo with 2 x 4^k / 32 AND + POPC per pair (lane = tentative, no table
 // lookups, no bank conflicts) and decides every pair outside the gap; the few
-// pairs inside it go to k_bexact, which forms S itself.  The second level
+// pairs inside it go to k_bexact_t, which forms S itself.  The second level
 // keeps the gap small where one level leaves it wide (reads holding a large
 // share of the k-mer space, whose counts are mostly 1 or 2).
 
@@ -1396,52 +1398,176 @@ __global__ void __launch_bounds__(BitsSmem<K>::THREADS, 1) k_bfilter_bits(DevRea
     }
 }
 
-// The word sum S itself for the pairs k_bfilter_bits left open: one warp per
-// pair scatters the tentative's counts into a table in shared memory and
-// streams the candidate's (k-mer, count) entries against it.  (k = 7: tables
-// of 32 KB, four warps per CTA.)
-template <int K>
-constexpr int kExactThreads = K <= 6 ? kFilterThreads : 128;
+// The open pairs grouped by tentative.  In the early passes of long-read
+// jobs most pairs are open (477k of 668k in the seventh pass of the 200k-read
+// workload, ~4,600 per tentative); one table per pair would be zeroed and
+// refilled ~4,600 times per tentative.  A counting sort of the queue by tentative index
+// (k_amb_count, k_amb_scan, k_amb_place) lets k_bexact_t build each
+// tentative's table once per CTA for a run of its pairs.  The order of the
+// pairs inside a tentative's run does not matter: each decision is a pure
+// function of its pair.
+//
+// amb_idx holds four arrays of kMaxBatch + 1: per tentative the pair count
+// (kept zero between passes), the run offsets, the placement cursors and the
+// work items (runs of up to kExactChunk pairs), as exclusive prefix sums.
+constexpr int kExactChunk = 64;
+constexpr int kAmbThreads = 256;
 
-template <int K>
-__global__ void __launch_bounds__(kExactThreads<K>) k_bexact(DevReads R, RoundState* st,
-                                                           const Pair* __restrict__ amb,
-                                                           int amb_cap, Pair* pairs, int seg_cap) {
-    constexpr int NB = 1 << (2 * K);
-    constexpr int WARPS = kExactThreads<K> / 32;  // one NB-entry table each
-    extern __shared__ __align__(16) uint16_t xtab[];  // [WARPS][NB]
+__device__ __forceinline__ int amb_n(const RoundState* st, int amb_cap) {
+    return min(st->n_amb, amb_cap);
+}
+
+// Per-CTA histogram of the open pairs' tentatives, added into the global one.
+__global__ void __launch_bounds__(kAmbThreads) k_amb_count(RoundState* st, const Pair* __restrict__ amb,
+                                                          int amb_cap, const uint32_t* __restrict__ tidx,
+                                                          int* amb_idx) {
+    __shared__ int h[kMaxBatch];
     if (st->done || st->n_tent == 0) return;
-    const int na = min(st->n_amb, amb_cap);
+    const int na = amb_n(st, amb_cap);
     if (na <= 0) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint16_t* tab = xtab + warp * NB;
-    unsigned n_al = 0;
-    for (int k = blockIdx.x * WARPS + warp; k < na; k += gridDim.x * WARPS) {
+    const int nt = st->n_tent;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) h[t] = 0;
+    __syncthreads();
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < na; k += gridDim.x * blockDim.x)
+        atomicAdd(&h[tidx[amb[k].rep] & 0xfff], 1);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nt; t += blockDim.x)
+        if (h[t]) atomicAdd(&amb_idx[t], h[t]);
+}
+
+// One CTA of 1,024 threads: run offsets, cursors and work items; the counts
+// go back to zero for the next pass.
+__global__ void __launch_bounds__(1024) k_amb_scan(RoundState* st, int amb_cap, int* amb_idx) {
+    __shared__ int ws[2][32];
+    if (st->done || st->n_tent == 0) return;
+    if (amb_n(st, amb_cap) <= 0) return;
+    const int nt = st->n_tent;
+    int* cnt = amb_idx;
+    int* off = amb_idx + (kMaxBatch + 1);
+    int* cur = amb_idx + 2 * (kMaxBatch + 1);
+    int* items = amb_idx + 3 * (kMaxBatch + 1);
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int c = t < nt ? cnt[t] : 0;
+    const int ch = (c + kExactChunk - 1) / kExactChunk;
+    int ic = c, ich = ch;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int a = __shfl_up_sync(kFull, ic, d), b = __shfl_up_sync(kFull, ich, d);
+        if (lane >= d) ic += a, ich += b;
+    }
+    if (lane == 31) ws[0][warp] = ic, ws[1][warp] = ich;
+    __syncthreads();
+    int bc = 0, bch = 0;
+    for (int w = 0; w < warp; w++) bc += ws[0][w], bch += ws[1][w];
+    const int ec = bc + ic - c, ech = bch + ich - ch;
+    if (t < nt) {
+        off[t] = ec;
+        cur[t] = ec;
+        items[t] = ech;
+        cnt[t] = 0;
+    }
+    if (t == nt - 1) {
+        off[nt] = ec + c;
+        items[nt] = ech + ch;
+    }
+}
+
+// Each CTA places a contiguous range of the queue: a shared histogram, one
+// global reservation per (CTA, tentative), then the pairs.
+__global__ void __launch_bounds__(kAmbThreads) k_amb_place(RoundState* st, const Pair* __restrict__ amb,
+                                                          int amb_cap, const uint32_t* __restrict__ tidx,
+                                                          int* amb_idx, Pair* amb2) {
+    __shared__ int h[kMaxBatch];
+    if (st->done || st->n_tent == 0) return;
+    const int na = amb_n(st, amb_cap);
+    if (na <= 0) return;
+    const int nt = st->n_tent;
+    int* cur = amb_idx + 2 * (kMaxBatch + 1);
+    const int per = (na + gridDim.x - 1) / gridDim.x;
+    const int lo = blockIdx.x * per, hi = min(na, lo + per);
+    if (lo >= hi) return;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) h[t] = 0;
+    __syncthreads();
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) atomicAdd(&h[tidx[amb[k].rep] & 0xfff], 1);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nt; t += blockDim.x)
+        if (h[t]) h[t] = atomicAdd(&cur[t], h[t]);
+    __syncthreads();
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
         const Pair p = amb[k];
-        uint4* t4 = reinterpret_cast<uint4*>(tab);
-        for (int i = lane; i < NB / 8; i += 32) t4[i] = make_uint4(0u, 0u, 0u, 0u);
-        __syncwarp();
-        const uint32_t* et = R.kmer + R.kmer_off[p.rep];
-        const int nt_ = R.n_kmer[p.rep];
-        for (int i = lane; i < nt_; i += 32) {
-            const uint32_t v = __ldg(et + i);
-            const uint32_t c = v & 0xffffu;
-            if (c) tab[v >> 16] = (uint16_t)c;  // kernel_makeTable: only order > 0
+        amb2[atomicAdd(&h[tidx[p.rep] & 0xfff], 1)] = p;
+    }
+}
+
+// The word sum S of the open pairs, run by run: a CTA takes a contiguous range
+// of work items, builds the tentative's count table in shared memory when the
+// tentative changes, and each warp streams one candidate's (k-mer, count)
+// entries against it (kernel_filter, func.cu:803-826).
+template <int K>
+__global__ void __launch_bounds__(kAmbThreads) k_bexact_t(DevReads R, RoundState* st,
+                                                        const Pair* __restrict__ amb2,
+                                                        const int* __restrict__ amb_idx,
+                                                        int amb_cap,
+                                                        const int32_t* __restrict__ tent,
+                                                        Pair* pairs, int seg_cap) {
+    constexpr int NB = 1 << (2 * K);
+    extern __shared__ __align__(16) uint16_t xtab[];  // NB counts
+    __shared__ int s_items[kMaxBatch + 1];
+    if (st->done || st->n_tent == 0) return;
+    if (amb_n(st, amb_cap) <= 0) return;
+    const int nt = st->n_tent;
+    const int* off = amb_idx + (kMaxBatch + 1);
+    const int* items = amb_idx + 3 * (kMaxBatch + 1);
+    for (int i = threadIdx.x; i <= nt; i += blockDim.x) s_items[i] = items[i];
+    __syncthreads();
+    const int total = s_items[nt];
+    const int per = (total + gridDim.x - 1) / gridDim.x;
+    const int i0 = blockIdx.x * per, i1 = min(total, i0 + per);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    unsigned n_al = 0;
+    int cur_t = -1;
+    for (int item = i0; item < i1; item++) {
+        // the tentative of this item: the last t with s_items[t] <= item
+        int lo = 0, hi = nt;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (s_items[mid] <= item) lo = mid;
+            else hi = mid;
         }
-        __syncwarp();
-        const uint32_t* eq = R.kmer + R.kmer_off[p.cand];
-        const int nq = R.n_kmer[p.cand];
-        int sum = 0;
-        for (int i = lane; i < nq; i += 32) {
-            const uint32_t v = __ldg(eq + i);
-            sum += min((uint32_t)tab[v >> 16], v & 0xffffu);
+        const int t = lo;
+        if (t != cur_t) {
+            __syncthreads();
+            uint4* t4 = reinterpret_cast<uint4*>(xtab);
+            for (int i = threadIdx.x; i < NB / 8; i += blockDim.x) t4[i] = make_uint4(0u, 0u, 0u, 0u);
+            __syncthreads();
+            const int rep = tent[t];
+            const uint32_t* et = R.kmer + R.kmer_off[rep];
+            const int ne = R.n_kmer[rep];
+            for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+                const uint32_t v = __ldg(et + i);
+                const uint32_t c = v & 0xffffu;
+                if (c) xtab[v >> 16] = (uint16_t)c;  // kernel_makeTable: only order > 0
+            }
+            __syncthreads();
+            cur_t = t;
         }
-        sum = warp_sum_i(sum);
-        if (!(sum < R.cut_word[p.cand])) {
-            if (lane == 0) push_pair(st, pairs, seg_cap, R, p.rep, p.cand, kBandMaxW);
-            n_al++;
+        const int k0 = off[t] + (item - s_items[t]) * kExactChunk;
+        const int k1 = min(off[t + 1], k0 + kExactChunk);
+        for (int k = k0 + warp; k < k1; k += warps) {
+            const Pair p = amb2[k];
+            const uint32_t* eq = R.kmer + R.kmer_off[p.cand];
+            const int nq = R.n_kmer[p.cand];
+            int sum = 0;
+            for (int i = lane; i < nq; i += 32) {
+                const uint32_t v = __ldg(eq + i);
+                sum += min((uint32_t)xtab[v >> 16], v & 0xffffu);
+            }
+            sum = warp_sum_i(sum);
+            if (!(sum < R.cut_word[p.cand])) {
+                if (lane == 0) push_pair(st, pairs, seg_cap, R, p.rep, p.cand, kBandMaxW);
+                n_al++;
+            }
         }
-        __syncwarp();
     }
     if (lane == 0 && n_al) atomicAdd(&st->cnt_aligned, (unsigned long long)n_al);
 }
@@ -1751,7 +1877,7 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
 // carry-save adders fill.  Since min(c_t, c_q) = [both >= 1] + (min - 1),
 //     D1 <= S <= D1 + min(E_t, E_q),   E = sum over k-mers of (count - 1),
 // so D1 >= cutoff passes a pair and D1 + min(E_t, E_q) < cutoff rejects it;
-// the pairs between go to k_bexact, which forms S itself.  Per pair the
+// the pairs between go to k_bexact_t, which forms S itself.  Per pair the
 // kernel reads one bit per candidate k-mer and spends about one instruction
 // per 32 pairs and k-mer, where the index form walks every shared k-mer's
 // posting.  A count never exceeds the candidate's k-mer entries, so eight
@@ -2463,40 +2589,51 @@ void launch_bfilter_idx_t(const DevReads& R, RoundBuffers& B, const int32_t* rem
     }
 }
 
+// The exact sums of the open pairs: the queue sorted by tentative, then one
+// table per run.
+template <int K>
+void launch_exact_t(const DevReads& R, RoundBuffers& B, cudaStream_t s) {
+    constexpr int xsmem = (1 << (2 * K)) * 2;
+    static int grid = 0;
+    if (!grid) {
+        cudaFuncSetAttribute(k_bexact_t<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, xsmem);
+        grid = grid_for(k_bexact_t<K>, kAmbThreads, xsmem, 8);
+    }
+    const int ga = num_sms() * 2;
+    k_amb_count<<<ga, kAmbThreads, 0, s>>>(B.st, B.amb, B.amb_cap, B.tidx, B.amb_idx);
+    k_amb_scan<<<1, 1024, 0, s>>>(B.st, B.amb_cap, B.amb_idx);
+    k_amb_place<<<ga, kAmbThreads, 0, s>>>(B.st, B.amb, B.amb_cap, B.tidx, B.amb_idx, B.amb2);
+    k_bexact_t<K><<<shaped(grid, R.filter_blocks), kAmbThreads, xsmem, s>>>(
+        R, B.st, B.amb2, B.amb_idx, B.amb_cap, B.tent, B.pairs, B.seg_cap);
+}
+
 template <int K>
 void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
                            cudaStream_t s) {
     // passes with one tentative (the first passes of adaptive R) go to the
     // plain kernel, which streams the candidates against one table
     launch_filter_t<K, false>(R, B, remain, s, B.tent);
-    constexpr int xsmem = (kExactThreads<K> / 32) * (1 << (2 * K)) * 2;
     constexpr int bsmem = (int)BitsSmem<K>::bytes;
     constexpr int bthreads = BitsSmem<K>::THREADS;
-    static int grid = 0, xgrid = 0;
+    static int grid = 0;
     if (!grid) {
         cudaFuncSetAttribute(k_bfilter_bits<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              bsmem);
-        cudaFuncSetAttribute(k_bexact<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, xsmem);
         grid = grid_for(k_bfilter_bits<K>, bthreads, bsmem, 2);
-        xgrid = grid_for(k_bexact<K>, kExactThreads<K>, xsmem, 8);
     }
     k_bfilter_bits<K><<<shaped(grid, R.filter_blocks), bthreads, bsmem, s>>>(
         R, B.st, remain, B.tent, B.pairs, B.seg_cap, B.amb, B.amb_cap);
-    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kExactThreads<K>, xsmem, s>>>(
-        R, B.st, B.amb, B.amb_cap, B.pairs, B.seg_cap);
+    launch_exact_t<K>(R, B, s);
 }
 
 template <int K>
 void launch_bfilter_mask_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
                            cudaStream_t s) {
-    constexpr int xsmem = (kExactThreads<K> / 32) * (1 << (2 * K)) * 2;
-    static int grid = 0, xgrid = 0;
+    static int grid = 0;
     if (!grid) {
-        cudaFuncSetAttribute(k_bexact<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, xsmem);
         cudaFuncSetAttribute(k_bfilter_mask, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              kMaskSmem);
         grid = grid_for(k_bfilter_mask, kMaskThreads, kMaskSmem, 2);
-        xgrid = grid_for(k_bexact<K>, kExactThreads<K>, xsmem, 8);
     }
     cudaMemsetAsync(B.tmask, 0, sizeof(uint4) * ((size_t)1 << (2 * K)) * B.tmask_rwq, s);
     k_bmask<<<kMaxBatch / 8, 256, 0, s>>>(R, B.st, B.tent, reinterpret_cast<uint32_t*>(B.tmask),
@@ -2504,8 +2641,7 @@ void launch_bfilter_mask_t(const DevReads& R, RoundBuffers& B, const int32_t* re
     k_bfilter_mask<<<shaped(grid, R.filter_blocks), kMaskThreads, kMaskSmem, s>>>(
         R, B.st, remain, B.tent, B.tmask, B.tmask_rwq, B.tmask_ex, B.pairs, B.seg_cap, B.amb,
         B.amb_cap);
-    k_bexact<K><<<shaped(xgrid, R.filter_blocks), kExactThreads<K>, xsmem, s>>>(
-        R, B.st, B.amb, B.amb_cap, B.pairs, B.seg_cap);
+    launch_exact_t<K>(R, B, s);
 }
 
 template <bool BATCH>
@@ -2683,6 +2819,8 @@ void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cud
     const int blocks = n > 0 ? (n + threads - 1) / threads : 1;
     k_init<<<blocks, threads, 0, s>>>(B.st, B.cluster, B.remain[0], B.tidx, B.best, n, batched,
                                       r_max, pass_limit, align_work_of(B.st));
+    // the open pairs' per-tentative counts start at zero (k_amb_scan keeps them so)
+    if (B.amb_idx) cudaMemsetAsync(B.amb_idx, 0, sizeof(int32_t) * (kMaxBatch + 1), s);
 }
 
 void resume_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
@@ -2694,6 +2832,7 @@ void resume_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, c
     k_resume_scan<<<blocks, 256, 0, s>>>(B.st, B.cluster, B.remain[0], B.tidx, B.best, n,
                                          batched);
     k_resume_start<<<1, 1, 0, s>>>(B.st, B.cluster, batched);
+    if (B.amb_idx) cudaMemsetAsync(B.amb_idx, 0, sizeof(int32_t) * (kMaxBatch + 1), s);
 }
 
 void launch_plain_round(const DevReads& R, RoundBuffers& B, int drop, int parity, cudaStream_t s,
@@ -2748,10 +2887,10 @@ void launch_batch_pass(const DevReads& R, RoundBuffers& B, int drop, int parity,
     if (ev4) cudaEventRecordWithFlags(ev4[3], s, cudaEventRecordExternal);
     if (count)
         *count += 8 + align_launches<true>(B) + (!drop ? 1 : 0) +
-                  (R.pig_q && !drop ? 1 : 0) + (B.amb && !drop ? 1 : 0);
-    // (a word-filter form launches two kernels, three with the open-pair
-    // queue: the bitmap form k_filter, k_bfilter_bits, k_bexact; the mask
-    // form k_bmask, k_bfilter_mask, k_bexact)
+                  (R.pig_q && !drop ? 1 : 0) + (B.amb && !drop ? 4 : 0);
+    // (a word-filter form launches two kernels, six with the open-pair
+    // queue: the bitmap form k_filter, k_bfilter_bits, the mask form k_bmask,
+    // k_bfilter_mask, then k_amb_count, k_amb_scan, k_amb_place, k_bexact_t)
 }
 
 // Whether a job's per-pass k-mer index (at most `cap` postings) is kept in
