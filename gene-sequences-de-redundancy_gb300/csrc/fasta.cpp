@@ -106,15 +106,24 @@ int parse_into(gsdr_fasta* f) {
     // reproduces the reference's order of equal-length reads; large inputs
     // run the same sort's independent parts on several threads (stdsort.h).
     const int32_t* dl = f->data_len.data();
-    gsdr::std_sort_threaded(f->order.begin(), f->order.end(),
-                            [dl](const int32_t& a, const int32_t& c) { return dl[a] > dl[c]; },
-                            gsdr::sort_threads());
     f->s_off.resize(count);
     f->s_len.resize(count);
-    for (int32_t i = 0; i < count; i++) {
-        f->s_off[i] = f->data_off[f->order[i]];
-        f->s_len[i] = f->data_len[f->order[i]];
-    }
+    // offsets and lengths in sorted order, gathered by the sort's own threads
+    const int32_t* ord = f->order.data();
+    const int64_t* doff = f->data_off.data();
+    int64_t* soff = f->s_off.data();
+    int32_t* slen = f->s_len.data();
+    const std::function<void(int, int)> gather = [=](int t, int T) {
+        const int32_t lo = (int32_t)((int64_t)count * t / T);
+        const int32_t hi = (int32_t)((int64_t)count * (t + 1) / T);
+        for (int32_t i = lo; i < hi; i++) {
+            soff[i] = doff[ord[i]];
+            slen[i] = dl[ord[i]];
+        }
+    };
+    gsdr::std_sort_threaded(f->order.begin(), f->order.end(),
+                            [dl](const int32_t& a, const int32_t& c) { return dl[a] > dl[c]; },
+                            gsdr::sort_threads(), gather);
     return GSDR_OK;
 }
 

@@ -35,6 +35,8 @@
 #pragma once
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
+#include <functional>
 #include <iterator>
 #include <mutex>
 #include <thread>
@@ -222,13 +224,18 @@ void team_sort(Team<It, Depth>& tm, int t, It first, It last, Depth depth0, C c)
 }  // namespace sort_detail
 #endif
 
+// after(t, T), if given, runs on every thread t of the T that sorted, once the
+// permutation is final (a parallel pass over the sorted range, e.g. a gather
+// by the permutation, on threads that already exist).
 template <class It, class Comp>
-void std_sort_threaded(It first, It last, Comp comp, int threads) {
+void std_sort_threaded(It first, It last, Comp comp, int threads,
+                       const std::function<void(int, int)>& after = {}) {
 #if defined(__GLIBCXX__)
     using Diff = typename std::iterator_traits<It>::difference_type;
     const Diff n = last - first;
     if (threads <= 1 || n < ((Diff)1 << 16)) {
         std::sort(first, last, comp);
+        if (after) after(0, 1);
         return;
     }
     // std::sort = std::__sort: the introsort loop with depth limit
@@ -247,25 +254,43 @@ void std_sort_threaded(It first, It last, Comp comp, int threads) {
             pool.emplace_back([&, t]() {
                 int g;
                 while ((g = go.load(std::memory_order_acquire)) == 0) std::this_thread::yield();
-                if (g > 0) sort_detail::team_sort(tm, t, first, last, depth0, c);
+                if (g > 0) {
+                    sort_detail::team_sort(tm, t, first, last, depth0, c);
+                    if (after) {
+                        tm.bar.wait();  // every part finished
+                        after(t, threads);
+                    }
+                }
             });
     } catch (...) {
         go.store(-1, std::memory_order_release);
         for (auto& th : pool) th.join();
         std::sort(first, last, comp);
+        if (after) after(0, 1);
         return;
     }
     go.store(1, std::memory_order_release);
     sort_detail::team_sort(tm, 0, first, last, depth0, c);
+    if (after) {
+        tm.bar.wait();
+        after(0, threads);
+    }
     for (auto& th : pool) th.join();
 #else
     (void)threads;
     std::sort(first, last, comp);
+    if (after) after(0, 1);
 #endif
 }
 
 // Threads for the host sort: the machine's cores, at most 16.
+// Threads of the host sort: the hardware threads, at most 16; GSDR_SORT_THREADS
+// overrides (1 = plain std::sort).
 inline int sort_threads() {
+    if (const char* e = std::getenv("GSDR_SORT_THREADS")) {
+        const int v = std::atoi(e);
+        if (v >= 1) return std::min(v, 64);
+    }
     const unsigned h = std::thread::hardware_concurrency();
     return h == 0 ? 1 : (int)std::min(h, 16u);
 }
