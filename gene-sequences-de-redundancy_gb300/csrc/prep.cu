@@ -23,9 +23,13 @@ namespace {
 constexpr int kPackWarps = 8;
 
 __device__ __forceinline__ int base_code(uint32_t b) {
-    // A/a->0, C/c->1, G/g->2, T/t/U/u->3, anything else->4 (func.cu:139-179).
-    uint32_t l = b | 0x20u;
-    return l == 'a' ? 0 : l == 'c' ? 1 : l == 'g' ? 2 : (l == 't' || l == 'u') ? 3 : 4;
+    // A/a->0, C/c->1, G/g->2, T/t/U/u->3, anything else->4 (func.cu:139-179),
+    // without branches: b | 0x20 is 'a' .. 'u' only for those letters' two
+    // cases (and for the other letters), and a 64-bit table holds the 3-bit
+    // codes of 'a' .. 'u' (21 entries: a 0, c 1, g 2, t 3, u 3, the rest 4)
+    constexpr unsigned long long kCodes = 0x37249249248a4860ull;
+    const uint32_t idx = (b | 0x20u) - 0x61u;
+    return idx < 21u ? (int)((kCodes >> (3u * idx)) & 7u) : 4;
 }
 
 __device__ __forceinline__ int warp_sum(int v) {
@@ -107,21 +111,25 @@ __global__ void __launch_bounds__(kPackWarps * 32) k_pack(DevReads R, float t, i
                 if (lane == 0) before = gap_before ? 1u : 0u;
                 gap_before = __shfl_sync(0xffffffffu, last_gap, 31) != 0;
             }
+            // the chunk holds read positions p0 .. p0 + 15; every step below is
+            // a select, not a branch (lanes see different bases)
+            const int p0 = (int)(16 * c - head);
+            const bool in_range = c < nchunks;
 #pragma unroll
             for (int jj = 0; jj < 16; jj++) {
-                const long long pos = 16 * c + jj - head;
-                const bool valid = (c < nchunks) && pos >= 0 && pos < L;
+                const int pos = p0 + jj;
+                const bool valid = in_range && pos >= 0 && pos < L;
                 const int code = valid ? base_code((words[jj >> 2] >> (8 * (jj & 3))) & 0xffu) : 4;
-                if (valid && code == 4) gaps |= 1u << jj;
-                if (code < 4) {
-                    if ((jj == 0 ? before : (gaps >> (jj - 1))) & 1u) marks |= 1u << nb;
-                    acc = (acc << 2) | (uint32_t)code;
-                    nb++;
-                    cnt0 += code == 0;
-                    cnt1 += code == 1;
-                    cnt2 += code == 2;
-                    cnt3 += code == 3;
-                }
+                gaps |= (valid && code == 4 ? 1u : 0u) << jj;
+                const bool ok = code < 4;
+                const uint32_t prev_gap = (jj == 0 ? before : (gaps >> (jj - 1))) & 1u;
+                marks |= ok && prev_gap ? 1u << nb : 0u;
+                acc = ok ? (acc << 2) | (uint32_t)code : acc;
+                nb += ok ? 1 : 0;
+                cnt0 += code == 0;
+                cnt1 += code == 1;
+                cnt2 += code == 2;
+                cnt3 += code == 3;
             }
 
             acc = nb ? (acc << (2 * (16 - nb))) : 0u;
