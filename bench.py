@@ -347,8 +347,20 @@ def serve_stream(jobs, gaps, device, max_inflight):
     import gsdr
 
     srv = gsdr.Server(device=device, max_inflight=max_inflight)
-    lat, status, run = {}, {}, {}
+    lat, status, run, results = {}, {}, {}, {}
     ids = []
+    first = set()  # the first three jobs: their results are kept for the oracle check
+
+    def done(r):
+        # a finished job's times, then its result released at once (a long
+        # stream would otherwise hold every job's output in host memory)
+        jid = r[0]
+        lat[jid], status[jid] = r[2], r[1]
+        run[jid] = srv.times(jid)[1]
+        if jid in first and r[1] == 0:
+            results[jid] = srv.result(jid)[1]
+        srv.release(jid)
+
     t0 = time.perf_counter()
     try:
         due = t0
@@ -361,21 +373,17 @@ def serve_stream(jobs, gaps, device, max_inflight):
                         break
                     r = srv.wait(int((due - now) * 1000) + 1)
                     if r:
-                        lat[r[0]], status[r[0]] = r[2], r[1]
-            ids.append((srv.submit(data, t), n))
+                        done(r)
+            jid = srv.submit(data, t)
+            if k < 3:
+                first.add(jid)
+            ids.append((jid, n))
         while len(lat) < len(ids):
             r = srv.wait(600000)
             if r is None:
                 break
-            lat[r[0]], status[r[0]] = r[2], r[1]
+            done(r)
         wall = time.perf_counter() - t0
-        for jid, _ in ids:
-            if jid in lat:
-                run[jid] = srv.times(jid)[1]
-        results = {jid: srv.result(jid)[1] for jid, _ in ids[:3] if status.get(jid) == 0}
-        for jid, _ in ids:
-            if jid in lat:
-                srv.release(jid)
     finally:
         srv.close()
     rows = [(status.get(j), lat.get(j), run.get(j), n, jobs[k][1]) for k, (j, n) in enumerate(ids)]
