@@ -21,6 +21,16 @@
 // runs alone, so every job is served.  Device memory comes from the library's
 // stream-ordered pool (devmem.h): a finished job's release waits for nothing
 // but its own stream.
+//
+// Order: when a slot is free the scheduler starts the smallest queued job (by
+// bytes, the measure of its parse and filter work), unless the job that has
+// waited longest has waited kAgeMs or more: then that one.  Short jobs no
+// longer queue behind long ones, and no job waits behind an endless run of
+// smaller ones.  A job whose threshold checkOption refuses is finished at
+// submission.  One slot beyond max_inflight, the express slot, takes only
+// jobs of at most express_bytes (4 MiB by default), so a short job need not
+// wait while every regular slot holds a long one.  The order changes no result: the jobs are
+// independent.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -56,6 +66,7 @@ struct ServerJob {
     int64_t parse_bytes = 0;  // step-1 reservation
     int64_t job_bytes = 0;    // step-2 reservation
     bool clustering = false;
+    bool express = false;     // runs in the express slot
 };
 
 }  // namespace gsdr
@@ -76,6 +87,7 @@ struct gsdr_server {
     std::thread scheduler;
     bool workers_stop = false;
     int inflight = 0;
+    int express = 0;                   // jobs in the express slot (0 or 1)
     int clustering = 0;                // jobs past step 2
     int64_t mem_used = 0;
     int64_t next_id = 1;
@@ -132,41 +144,71 @@ void run_job(gsdr_server* s, std::shared_ptr<ServerJob> j) {
     j->fasta.shrink_to_fit();
     std::lock_guard<std::mutex> lock(s->mu);
     s->inflight--;
+    if (j->express) s->express = 0;
     s->mem_used -= j->parse_bytes + j->job_bytes;
     if (j->clustering) s->clustering--;
     finish(s, j, rc);
     s->cv_sched.notify_all();
 }
 
+// A job that has waited this long goes before smaller ones.
+constexpr double kAgeMs = 1000.0;
+// Jobs of at most this many FASTA bytes may take the express slot (the
+// default of gsdr_server_opts.express_bytes).
+constexpr int64_t kExpressBytes = (int64_t)4 << 20;
+
+using JobIt = std::deque<std::shared_ptr<ServerJob>>::iterator;
+
+JobIt smallest_job(gsdr_server* s) {
+    auto& q = s->queue;
+    auto best = q.begin();
+    for (auto it = q.begin(); it != q.end(); ++it)
+        if ((*it)->fasta.size() < (*best)->fasta.size()) best = it;
+    return best;
+}
+
+// The queued job to start now, or the queue's end: with a regular slot free
+// the job that has waited kAgeMs or more (the queue is in submission order,
+// so its front has waited longest), else the smallest; with only the express
+// slot free the smallest, if it is short enough.
+JobIt next_job(gsdr_server* s) {
+    auto& q = s->queue;
+    if (q.empty()) return q.end();
+    if (s->inflight - s->express < s->so.max_inflight) {
+        if (now_ms() - q.front()->t_submit >= kAgeMs) return q.begin();
+        return smallest_job(s);
+    }
+    if (s->express == 0 && s->so.express_bytes > 0) {
+        auto it = smallest_job(s);
+        if ((int64_t)(*it)->fasta.size() <= s->so.express_bytes) return it;
+    }
+    return q.end();
+}
+
 void scheduler_loop(gsdr_server* s) {
     cudaSetDevice(s->so.device);
     while (true) {
+        std::unique_lock<std::mutex> lock(s->mu);
+        // the choice is made when a slot is free, among the jobs queued then
+        s->cv_sched.wait(lock, [&] { return s->stopping || next_job(s) != s->queue.end(); });
+        if (s->stopping && s->queue.empty()) return;
         std::shared_ptr<ServerJob> j;
-        {
-            std::unique_lock<std::mutex> lock(s->mu);
-            s->cv_sched.wait(lock, [&] { return s->stopping || !s->queue.empty(); });
-            if (s->stopping && s->queue.empty()) return;
+        if (s->stopping) {
             j = s->queue.front();
             s->queue.pop_front();
-        }
-        gsdr_opts o;
-        gsdr_default_opts(&o);
-        o.threshold = j->threshold;
-        o.batch = s->so.batch;
-        const int rc = gsdr_resolve_opts(&o, nullptr);
-        std::unique_lock<std::mutex> lock(s->mu);
-        if (rc) {  // t outside [0.8, 1): refused as checkOption refuses it
-            j->error = gsdr_last_error();
-            finish(s, j, rc);
-            continue;
+        } else {
+            auto it = next_job(s);
+            j = *it;
+            s->queue.erase(it);
+            j->express = s->inflight - s->express >= s->so.max_inflight;
         }
         j->parse_bytes = cluster_fasta_parse_bytes((int64_t)j->fasta.size(), j->records,
                                                    j->newlines);
-        // step 1: a free slot and room for the parse buffers (or nothing running)
+        // step 1: room for the parse buffers (or nothing running); the slot
+        // was free when the job was chosen and only this thread takes slots
         s->cv_sched.wait(lock, [&] {
-            return s->stopping || (s->inflight < s->so.max_inflight &&
-                                   (s->mem_used + j->parse_bytes <= s->so.mem_budget ||
-                                    s->inflight == 0));
+            return s->stopping ||
+                   s->mem_used + j->parse_bytes <= s->so.mem_budget || s->inflight == 0;
         });
         if (s->stopping) {
             j->error = "server stopped";
@@ -174,6 +216,7 @@ void scheduler_loop(gsdr_server* s) {
             continue;
         }
         s->inflight++;
+        if (j->express) s->express = 1;
         s->mem_used += j->parse_bytes;
         s->ready.push_back(j);
         s->cv_work.notify_one();
@@ -210,6 +253,7 @@ int gsdr_server_create(const gsdr_server_opts* so, gsdr_server** out) {
     if (!s) return fail(GSDR_ENOMEM, "server: out of host memory");
     s->so = *so;
     if (s->so.max_inflight <= 0) s->so.max_inflight = 4;
+    if (s->so.express_bytes == 0) s->so.express_bytes = kExpressBytes;
     if (s->so.mem_budget <= 0) {
         size_t free_b = 0, total_b = 0;
         cudaSetDevice(so->device);
@@ -219,7 +263,8 @@ int gsdr_server_create(const gsdr_server_opts* so, gsdr_server** out) {
         }
         s->so.mem_budget = (int64_t)(free_b / 10 * 8);
     }
-    for (int w = 0; w < s->so.max_inflight; w++) s->workers.emplace_back(worker_loop, s);
+    // a worker per slot, the express slot included
+    for (int w = 0; w <= s->so.max_inflight; w++) s->workers.emplace_back(worker_loop, s);
     s->scheduler = std::thread(scheduler_loop, s);
     *out = s;
     return GSDR_OK;
@@ -240,12 +285,28 @@ int gsdr_server_submit(gsdr_server* s, const char* fasta, int64_t n, float thres
     j->newlines = (int64_t)std::count(j->fasta.begin(), j->fasta.end(), '\n');
     j->threshold = threshold;
     j->t_submit = now_ms();
+    // t outside [0.8, 1): the job is refused as checkOption refuses it, at once
+    gsdr_opts o;
+    gsdr_default_opts(&o);
+    o.threshold = threshold;
+    o.batch = s->so.batch;
+    const int refused = gsdr_resolve_opts(&o, nullptr);
+    if (refused) {
+        j->error = gsdr_last_error();
+        j->fasta.clear();
+        j->fasta.shrink_to_fit();
+    }
     std::lock_guard<std::mutex> lock(s->mu);
     if (s->stopping) return fail(GSDR_EBUSY, "server: stopping");
     j->id = s->next_id++;
     s->jobs[j->id] = j;
-    s->queue.push_back(j);
     *job = j->id;
+    if (refused) {
+        j->t_start = j->t_submit;
+        finish(s, j, refused);
+        return GSDR_OK;
+    }
+    s->queue.push_back(j);
     s->cv_sched.notify_all();
     return GSDR_OK;
 }

@@ -101,6 +101,7 @@ class ServerOpts(C.Structure):
         ("max_inflight", C.c_int32),
         ("mem_budget", C.c_int64),
         ("batch", C.c_int32),
+        ("express_bytes", C.c_int64),
     ]
 
 
@@ -560,8 +561,8 @@ def set_spin_limit(polls, device=0):
 class Server:
     """Continuous batching of clustering jobs on one GPU (gsdr_server_*)."""
 
-    def __init__(self, device=0, max_inflight=4, mem_budget=0, batch=0):
-        so = ServerOpts(device, max_inflight, mem_budget, batch)
+    def __init__(self, device=0, max_inflight=4, mem_budget=0, batch=0, express_bytes=0):
+        so = ServerOpts(device, max_inflight, mem_budget, batch, express_bytes)
         h = C.c_void_p()
         _check(lib().gsdr_server_create(C.byref(so), C.byref(h)))
         self._h = h

@@ -307,6 +307,8 @@ typedef struct {
     int32_t max_inflight;     /* concurrent jobs on the device (streams) */
     int64_t mem_budget;       /* device bytes for job data; 0 = 80% of free memory */
     int32_t batch;            /* as gsdr_opts.batch */
+    int64_t express_bytes;    /* one slot beyond max_inflight takes only jobs of at most
+                                 this many FASTA bytes; 0 = 4 MiB, -1 = no such slot */
 } gsdr_server_opts;
 int gsdr_server_create(const gsdr_server_opts* so, gsdr_server** out);
 /* Submit a job: the FASTA bytes are copied; t as in gsdr_opts.  Returns the
