@@ -74,12 +74,24 @@ __global__ void k_nl_count(const uint8_t* __restrict__ b, int64_t n, int64_t n_c
          c += nw) {
         const int64_t base = c * kChunk;
         uint32_t k = 0;
-        for (int i = lane * 4; i < kChunk; i += 128) {
-            const int64_t p = base + i;
-            if (p + 4 <= n) {
-                k += __popc(nl_bytes(*reinterpret_cast<const uint32_t*>(b + p)));
-            } else {
-                for (int64_t q = p; q < n && q < p + 4; q++) k += b[q] == '\n';
+        if (base + kChunk <= n) {
+            // a whole chunk: 16 bytes per lane, all of the chunk's loads at once
+            const uint4* v4 = reinterpret_cast<const uint4*>(b + base) + lane;
+            uint4 v[kChunk / 512];
+#pragma unroll
+            for (int i = 0; i < kChunk / 512; i++) v[i] = __ldg(v4 + 32 * i);
+#pragma unroll
+            for (int i = 0; i < kChunk / 512; i++)
+                k += __popc(nl_bytes(v[i].x)) + __popc(nl_bytes(v[i].y)) +
+                     __popc(nl_bytes(v[i].z)) + __popc(nl_bytes(v[i].w));
+        } else {
+            for (int i = lane * 4; i < kChunk; i += 128) {
+                const int64_t p = base + i;
+                if (p + 4 <= n) {
+                    k += __popc(nl_bytes(*reinterpret_cast<const uint32_t*>(b + p)));
+                } else {
+                    for (int64_t q = p; q < n && q < p + 4; q++) k += b[q] == '\n';
+                }
             }
         }
         k = __reduce_add_sync(0xffffffffu, k);
@@ -96,6 +108,40 @@ __global__ void k_nl_write(const uint8_t* __restrict__ b, int64_t n, int64_t n_c
     for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_chunks;
          c += nw) {
         uint32_t at = base[c];
+        if ((c + 1) * kChunk <= n) {
+            // a whole chunk: 16 bytes per lane per step, the steps' loads at once
+            const uint4* v4 = reinterpret_cast<const uint4*>(b + c * kChunk) + lane;
+            uint4 v[kChunk / 512];
+#pragma unroll
+            for (int i = 0; i < kChunk / 512; i++) v[i] = __ldg(v4 + 32 * i);
+#pragma unroll
+            for (int i = 0; i < kChunk / 512; i++) {
+                const int64_t p = c * kChunk + 512 * i + 16 * lane;
+                const uint32_t w[4] = {v[i].x, v[i].y, v[i].z, v[i].w};
+                uint32_t m = 0;  // bit j: byte p + j is '\n'
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const uint32_t f = nl_bytes(w[h]);
+                    m |= (((f >> 7) & 1u) | ((f >> 14) & 2u) | ((f >> 21) & 4u) |
+                          ((f >> 28) & 8u)) << (4 * h);
+                }
+                const uint32_t k = __popc(m);
+                uint32_t incl = k;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+                    if (lane >= d) incl += o;
+                }
+                uint32_t wpos = at + incl - k;
+                while (m) {
+                    const int j = __ffs(m) - 1;
+                    m &= m - 1;
+                    nl[wpos++] = p + j;
+                }
+                at += __shfl_sync(0xffffffffu, incl, 31);
+            }
+            continue;
+        }
         for (int i = 0; i < kChunk; i += 128) {
             const int64_t p = c * kChunk + i + lane * 4;
             uint32_t m = 0;  // bit j: byte p + j is '\n'
