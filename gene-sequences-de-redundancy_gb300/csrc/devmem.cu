@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -87,6 +88,31 @@ void pinned_release(void* p) {
     if (!p) return;
     std::lock_guard<std::mutex> lock(g_pin_mu);
     g_pin_free.push_back(p);
+}
+
+namespace {
+struct PinnedScratch {
+    void* p = nullptr;
+    size_t cap = 0;
+    ~PinnedScratch() {
+        if (p) cudaFreeHost(p);
+    }
+};
+}  // namespace
+
+void* pinned_scratch(size_t bytes) {
+    static thread_local PinnedScratch s;
+    if (bytes <= s.cap) return s.p;
+    if (s.p) cudaFreeHost(s.p);
+    s.p = nullptr;
+    s.cap = 0;
+    const size_t want = std::max(bytes, (size_t)1 << 20);
+    if (cudaHostAlloc(&s.p, want, cudaHostAllocPortable) != cudaSuccess) {
+        s.p = nullptr;
+        return nullptr;
+    }
+    s.cap = want;
+    return s.p;
 }
 
 }  // namespace gsdr

@@ -30,4 +30,10 @@ constexpr size_t kPinnedSlot = 1024;
 void* pinned_slot();
 void pinned_release(void* p);
 
+// A pinned host buffer of at least `bytes`, owned by the calling thread and
+// reused by its later calls (grown when a call needs more; released when the
+// thread ends).  Its contents last until the thread's next call.  nullptr when
+// pinned memory cannot be had.
+void* pinned_scratch(size_t bytes);
+
 }  // namespace gsdr

@@ -535,13 +535,31 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     }
     DCUDA(cudaGetLastError());
     mark("parse");
-    std::vector<int64_t> h_dlen(n_rec), h_doff(n_rec);
-    std::vector<int32_t> h_pieces(n_rec);
-    DCUDA(cudaMemcpyAsync(h_dlen.data(), data_len.p, sizeof(int64_t) * n_rec,
+    // the record lengths, offsets and piece counts, in the thread's pinned
+    // scratch (a direct copy; pageable memory would take a staged one)
+    std::vector<int64_t> v_dlen, v_doff;
+    std::vector<int32_t> v_pieces;
+    int64_t* h_dlen = nullptr;
+    int64_t* h_doff = nullptr;
+    int32_t* h_pieces = nullptr;
+    if (char* pin = static_cast<char*>(pinned_scratch(sizeof(int64_t) * 2 * n_rec +
+                                                      sizeof(int32_t) * n_rec))) {
+        h_dlen = reinterpret_cast<int64_t*>(pin);
+        h_doff = h_dlen + n_rec;
+        h_pieces = reinterpret_cast<int32_t*>(h_doff + n_rec);
+    } else {
+        v_dlen.resize(n_rec);
+        v_doff.resize(n_rec);
+        v_pieces.resize(n_rec);
+        h_dlen = v_dlen.data();
+        h_doff = v_doff.data();
+        h_pieces = v_pieces.data();
+    }
+    DCUDA(cudaMemcpyAsync(h_dlen, data_len.p, sizeof(int64_t) * n_rec,
                           cudaMemcpyDeviceToHost, s));
-    DCUDA(cudaMemcpyAsync(h_doff.data(), data_off.p, sizeof(int64_t) * n_rec,
+    DCUDA(cudaMemcpyAsync(h_doff, data_off.p, sizeof(int64_t) * n_rec,
                           cudaMemcpyDeviceToHost, s));
-    DCUDA(cudaMemcpyAsync(h_pieces.data(), pieces.p, sizeof(int32_t) * n_rec,
+    DCUDA(cudaMemcpyAsync(h_pieces, pieces.p, sizeof(int32_t) * n_rec,
                           cudaMemcpyDeviceToHost, s));
     DCUDA(cudaStreamSynchronize(s));
     // multi-line records: data placed end to end after the file
@@ -556,7 +574,7 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
         }
     }
     if (multi) {
-        DCUDA(cudaMemcpyAsync(data_off.p, h_doff.data(), sizeof(int64_t) * n_rec,
+        DCUDA(cudaMemcpyAsync(data_off.p, h_doff, sizeof(int64_t) * n_rec,
                               cudaMemcpyHostToDevice, s));
         k_rec_concat<<<grid_of(n_rec, 8, 1 << 16), 256, 0, s>>>(
             b, nl.as<int64_t>(), n_nl, n, n_lines, head.as<int64_t>(), n_rec,
@@ -571,14 +589,14 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     mark("records");
     // (the record lengths are below 2^31, so comparing them as 64-bit values
     // gives the comparator's outcomes, hence the permutation, of 32-bit ones)
-    const int64_t* dlp = h_dlen.data();
+    const int64_t* dlp = h_dlen;
     std::vector<int64_t> s_off(nr);
     res->length.resize(nr);
     // offsets and lengths in sorted order, gathered by the sort's own threads
     // (one thread takes ~1 ms for the 200k-read workload: random reads of
     // arrays the copy wrote)
     const int32_t* ord = res->order.data();
-    const int64_t* doff = h_doff.data();
+    const int64_t* doff = h_doff;
     int64_t* soff = s_off.data();
     int32_t* slen = res->length.data();
     const std::function<void(int, int)> gather = [=](int t, int T) {
