@@ -103,7 +103,7 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
     P.variant = o.variant;
     P.r_max = (o.batch == 1 || (!drop && k >= kWideK)) ? 1 : job_r_max(o);
     const int64_t kcap = (int64_t)1 << (2 * (k > 0 ? k : 1));
-    int64_t ents_sum = 0, ents_max = 0;
+    int64_t ents_sum = 0, ents_max = 0, pack_run = 0, kmer_run = 0;
     std::vector<int64_t> head;  // entries of the first kMaxBatch reads, prefix sums
     head.reserve(kMaxBatch + 1);
     head.push_back(0);
@@ -115,14 +115,18 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
             return fail(GSDR_EINVAL, "read outside the byte buffer");
         if (L > P.max_len) P.max_len = L;
         if (i > 0 && L > reads->length[i - 1]) sorted = false;
-        P.pack_off[i + 1] = P.pack_off[i] + round4(L / 16 + 1);
+        // (the running offsets stay in registers: reading back the entry just
+        // stored would chain every iteration on a store-to-load forward)
+        pack_run += round4(L / 16 + 1);
+        P.pack_off[i + 1] = pack_run;
         int64_t ents = drop ? 0 : L - k + 1;
         if (ents < 0) ents = 0;
         if (ents > kcap) ents = kcap;
         ents_sum += ents;
         if (ents > ents_max) ents_max = ents;
         if (i < kMaxBatch) head.push_back(head.back() + ents);
-        P.kmer_off[i + 1] = P.kmer_off[i] + round4(ents);
+        kmer_run += round4(ents);
+        P.kmer_off[i + 1] = kmer_run;
     }
     if (o.pigeon == 1 && !drop) {
         P.refoff16.resize(n);
