@@ -1878,9 +1878,9 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
 //     D1 <= S <= D1 + min(E_t, E_q),   E = sum over k-mers of (count - 1),
 // so D1 >= cutoff passes a pair and D1 + min(E_t, E_q) < cutoff rejects it;
 // the pairs between go to k_bexact_t, which forms S itself.  Per pair the
-// kernel reads one bit per candidate k-mer and spends about one instruction
-// per 32 pairs and k-mer, where the index form walks every shared k-mer's
-// posting.  A count never exceeds the candidate's k-mer entries, so eight
+// kernel reads one bit per candidate k-mer and spends about three logic
+// instructions per 32 pairs and k-mer, where the index form takes a warp
+// step per posting of every shared k-mer.  A count never exceeds the candidate's k-mer entries, so eight
 // planes hold it: the form runs only where every read has at most
 // kMaskMaxEntries entries.
 
@@ -1997,9 +1997,9 @@ __device__ __forceinline__ void cp_async_wait() {
 // LPR, works for candidate g of the warp's 32 / LPR consecutive candidates
 // (consecutive in the remain list, so of similar length) and holds the counts
 // of word x of the rows (tentatives 128 x .. 128 x + 127).  Each step a group
-// copies the rows of 8 of its candidate's k-mers; the entries of the step
-// after next load one step ahead of their copies, the copies kMaskStages - 1
-// steps ahead of their counts.
+// copies the rows of 8 of its candidate's k-mers; a step's entries load two
+// issues before its copies, and the copies kMaskStages - 1 steps before their
+// counts.
 template <int LPR>
 __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* st,
                                                 const int32_t* __restrict__ remain,
