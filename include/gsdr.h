@@ -300,7 +300,10 @@ const char* gsdr_last_error(void);
 /* ---- Serving: continuous batching of independent clustering jobs ----------
  * No counterpart in the reference.  Jobs are admitted by device-memory
  * footprint, run concurrently on separate CUDA streams, and each job's result
- * equals what gsdr_cluster returns for it alone. */
+ * equals what gsdr_cluster returns for it alone.  When a slot frees, the
+ * smallest queued job starts (a job that has waited 1 s or more goes first);
+ * a job with a threshold checkOption refuses finishes with GSDR_EINVAL at
+ * submission. */
 typedef struct gsdr_server gsdr_server;
 typedef struct {
     int32_t device;
