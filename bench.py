@@ -179,11 +179,12 @@ def filter_roofline(r, figures):
     kernel = {"table": "k_bfilter_tab (per-tentative k-mer tables in shared memory, "
                        "transposed, paired 16-bit min/add)",
               "index": "k_bindex + k_bfilter_idx (inverted k-mer index in shared memory)",
-              "bits": "k_bfilter_bits + k_bexact (two-level k-mer count bitmaps: AND + POPC "
-                      "per tentative, exact sums for the pairs the bound leaves open)",
-              "masks": "k_bmask + k_bfilter_mask + k_bexact (per-k-mer rows of tentative bits "
-                       "in L2, bit-sliced counts per candidate, exact sums for the pairs the "
-                       "bound leaves open)"}[form]
+              "bits": "k_bfilter_bits + k_bexact_t (two-level k-mer count bitmaps: AND + POPC "
+                      "per tentative, exact sums for the pairs the bound leaves open, grouped "
+                      "by tentative)",
+              "masks": "k_bmask + k_bfilter_mask + k_bexact_t (per-k-mer rows of tentative "
+                       "bits in L2, bit-sliced counts per candidate, exact sums for the pairs "
+                       "the bound leaves open, grouped by tentative)"}[form]
     ratio = figures.get("c%d.filter_%s.dram_over_input" % (r["config"], form))
     return {"bound": "hbm", "kernel": kernel,
             "achieved": achieved, "peak": r["peak"], "unit": "GB/s",
