@@ -1,12 +1,15 @@
 // The team sort of csrc/stdsort.h against std::sort on seeded random inputs:
-// the permutations must be identical (ties included).  Built and run by
-// tests/test_stdsort.py; prints the number of mismatches and exits non-zero
-// on any.
+// the permutations must be identical (ties included), and the pass it runs
+// on its threads after sorting (a gather by the permutation, as the FASTA
+// readers use it) must see the final permutation and cover every position
+// once.  Built and run by tests/test_stdsort.py; prints the number of
+// mismatches and exits non-zero on any.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <numeric>
 #include <random>
 #include <vector>
@@ -41,10 +44,28 @@ int main(int argc, char** argv) {
         auto longer_first = [k](const int32_t& x, const int32_t& y) { return k[x] > k[y]; };
         std::sort(a.begin(), a.end(), longer_first);
         const int threads = 2 + (int)(rng() % 15);
-        gsdr::std_sort_threaded(b.begin(), b.end(), longer_first, threads);
-        if (a != b) {
+        std::vector<int32_t> gathered(n, -1);
+        std::vector<int> visits(n, 0);
+        const int32_t* pb = b.data();
+        int32_t* pg = gathered.data();
+        int* pv = visits.data();
+        const std::function<void(int, int)> gather = [=](int t, int T) {
+            const int lo = (int)((int64_t)n * t / T), hi = (int)((int64_t)n * (t + 1) / T);
+            for (int i = lo; i < hi; i++) {
+                pg[i] = k[pb[i]];
+                pv[i]++;
+            }
+        };
+        gsdr::std_sort_threaded(b.begin(), b.end(), longer_first, threads,
+                                trial % 2 ? gather : std::function<void(int, int)>());
+        bool gather_ok = true;
+        if (trial % 2)
+            for (int i = 0; i < n; i++)
+                if (visits[i] != 1 || gathered[i] != key[a[i]]) gather_ok = false;
+        if (a != b || !gather_ok) {
             bad++;
-            std::printf("mismatch: trial %d n %d mode %d threads %d\n", trial, n, mode, threads);
+            std::printf("mismatch: trial %d n %d mode %d threads %d gather %d\n", trial, n, mode,
+                        threads, (int)gather_ok);
         }
     }
     std::printf("mismatches %d of %d\n", bad, trials);
