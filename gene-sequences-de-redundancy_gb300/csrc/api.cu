@@ -73,6 +73,7 @@ struct Plan {
     bool idx_smem = false;  // that index fits the filter's shared memory (16-bit copy)
     bool bits = false;      // batched word filter by k-mer presence bitmaps
     bool masks = false;     // batched word filter by tentative masks
+    int mask_planes = 8;    // their count planes (10 where a read has over 255 entries)
     // pigeon filter (p 1): low 16 bits of each read's offset in the
     // reference's padded layout (copyData, func.cu:119-137: L/16*16 + 16 per read)
     std::vector<uint16_t> refoff16;
@@ -144,9 +145,10 @@ int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
         // reads and 82 against 298 ms at 50k, 10k reads of 200-1,000 bp 7.0
         // against 8.4 ms)
         bool bits = !index && k <= kMaxBits2K;
-        // sparse spaces with short reads: the tentative masks, whose 8-plane
-        // counts hold reads of at most 255 k-mers
+        // sparse spaces with short reads: the tentative masks, whose counts
+        // (8 or 10 bit planes) hold reads of at most kMaskMaxEntries k-mers
         const bool masks_ok = k <= kMaxBits2K && ents_max <= kMaskMaxEntries;
+        P.mask_planes = ents_max <= kMaskEntries8 ? 8 : 10;
         bool masks = index && masks_ok;
         // the caller's choice (word_filter), else GSDR_BFILTER=table|index|bits|masks
         int form = o.word_filter;
@@ -251,6 +253,7 @@ size_t carve_all(char* base, int n, int64_t n_bytes, const Plan& P, bool drop, i
     B.amb2 = P.bits || P.masks ? c.take<Pair>((size_t)B.amb_cap) : nullptr;
     B.amb_idx = P.bits || P.masks ? c.take<int32_t>(4 * (size_t)(kMaxBatch + 1)) : nullptr;
     B.tmask_rwq = P.masks ? (P.r_max + 127) / 128 : 0;
+    B.tmask_planes = P.mask_planes;
     B.tmask = P.masks ? c.take<uint4>(((size_t)1 << (2 * k)) * B.tmask_rwq) : nullptr;
     B.tmask_ex = P.masks ? c.take<int32_t>(kMaxBatch) : nullptr;
     // word lengths 8..12: k-mer ids and counts apart, the global table, the

@@ -39,7 +39,8 @@ constexpr int kMaxBatch = 1024;         // tentative representatives per batched
 constexpr int kTTWords = kMaxBatch / 32;
 constexpr int kMaxBitsK = 6;            // k-mer presence bitmaps for k <= 6 (4^k bits per read)
 constexpr int kMaxBits2K = 7;           // the batched two-level bitmap filter: k <= 7
-constexpr int kMaskMaxEntries = 255;    // tentative-mask filter: reads of at most 255 k-mers
+constexpr int kMaskMaxEntries = 1023;   // tentative-mask filter: reads of at most 1,023 k-mers
+constexpr int kMaskEntries8 = 255;      // ... with eight count planes up to 255, else ten
 
 struct Pair {
     int32_t rep;   // read index of the representative (or tentative)
@@ -218,6 +219,7 @@ struct RoundBuffers {
     uint4* tmask;        // 4^k rows
     int32_t* tmask_ex;   // kMaxBatch
     int32_t tmask_rwq;   // 16-byte words per row: ceil(r_max / 128)
+    int32_t tmask_planes;  // count planes: 8 (every read <= kMaskEntries8 entries) or 10
 };
 void init_rounds(const DevReads& R, RoundBuffers& B, int batched, int r_max, cudaStream_t s,
                  int pass_limit = 0);

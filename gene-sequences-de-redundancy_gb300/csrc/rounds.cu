@@ -1880,9 +1880,9 @@ __global__ void __launch_bounds__(1024, 1) k_bfilter_idx(
 // the pairs between go to k_bexact_t, which forms S itself.  Per pair the
 // kernel reads one bit per candidate k-mer and spends about three logic
 // instructions per 32 pairs and k-mer, where the index form takes a warp
-// step per posting of every shared k-mer.  A count never exceeds the candidate's k-mer entries, so eight
-// planes hold it: the form runs only where every read has at most
-// kMaskMaxEntries entries.
+// step per posting of every shared k-mer.  A count never exceeds the
+// candidate's k-mer entries: eight planes hold it where every read has at
+// most kMaskEntries8 entries, ten up to kMaskMaxEntries (the form's limit).
 
 constexpr int kMaskThreads = 256;
 
@@ -1915,12 +1915,13 @@ __global__ void __launch_bounds__(256) k_bmask(DevReads R, RoundState* st,
     }
 }
 
-// p += w0 + .. + w7, bit-sliced (8 planes, counts below 256), in two parts:
+// p += w0 + .. + w7, bit-sliced (NP planes, counts below 2^NP), in two parts:
 // a Harley-Seal tree of carry-save adders into the planes of weight 1, 2 and
 // 4 that returns the carry of weight 8, and bs_carry, which adds a carry
 // into the planes from `from` up.  Two trees' carries meet in one more adder
 // first (bs_pair8), so the ripple runs once per 16 words.
-__device__ __forceinline__ uint32_t bs_tree8(uint32_t (&p)[8], uint32_t w0, uint32_t w1,
+template <int NP>
+__device__ __forceinline__ uint32_t bs_tree8(uint32_t (&p)[NP], uint32_t w0, uint32_t w1,
                                              uint32_t w2, uint32_t w3, uint32_t w4, uint32_t w5,
                                              uint32_t w6, uint32_t w7) {
     uint32_t t1, t2, t3, t4, f1, f2, e8;
@@ -1933,9 +1934,10 @@ __device__ __forceinline__ uint32_t bs_tree8(uint32_t (&p)[8], uint32_t w0, uint
     csa(p[2], e8, p[2], f1, f2);
     return e8;
 }
-__device__ __forceinline__ void bs_carry(uint32_t (&p)[8], int from, uint32_t c) {
+template <int NP>
+__device__ __forceinline__ void bs_carry(uint32_t (&p)[NP], int from, uint32_t c) {
 #pragma unroll
-    for (int b = 0; b < 8; b++) {
+    for (int b = 0; b < NP; b++) {
         if (b < from) continue;
         const uint32_t t = p[b] & c;
         p[b] ^= c;
@@ -1943,19 +1945,21 @@ __device__ __forceinline__ void bs_carry(uint32_t (&p)[8], int from, uint32_t c)
     }
 }
 // Two weight-8 carries: one adder into plane 3, its weight-16 carry rippled.
-__device__ __forceinline__ void bs_pair8(uint32_t (&p)[8], uint32_t a8, uint32_t b8) {
+template <int NP>
+__device__ __forceinline__ void bs_pair8(uint32_t (&p)[NP], uint32_t a8, uint32_t b8) {
     uint32_t c16;
     csa(p[3], c16, p[3], a8, b8);
-    bs_carry(p, 4, c16);
+    bs_carry<NP>(p, 4, c16);
 }
 
 // Bits of the counts >= v.
-__device__ __forceinline__ uint32_t bs_ge(const uint32_t (&p)[8], int v) {
+template <int NP>
+__device__ __forceinline__ uint32_t bs_ge(const uint32_t (&p)[NP], int v) {
     if (v <= 0) return 0xffffffffu;
-    if (v > 255) return 0u;
+    if (v > (1 << NP) - 1) return 0u;
     uint32_t gt = 0, eq = 0xffffffffu;
 #pragma unroll
-    for (int b = 7; b >= 0; b--) {
+    for (int b = NP - 1; b >= 0; b--) {
         const uint32_t vb = ((v >> b) & 1) ? 0xffffffffu : 0u;
         gt |= eq & p[b] & ~vb;
         eq &= ~(p[b] ^ vb);
@@ -1963,10 +1967,11 @@ __device__ __forceinline__ uint32_t bs_ge(const uint32_t (&p)[8], int v) {
     return gt | eq;
 }
 
-__device__ __forceinline__ int bs_get(const uint32_t (&p)[8], int bit) {
+template <int NP>
+__device__ __forceinline__ int bs_get(const uint32_t (&p)[NP], int bit) {
     int v = 0;
 #pragma unroll
-    for (int b = 0; b < 8; b++) v |= (int)((p[b] >> bit) & 1u) << b;
+    for (int b = 0; b < NP; b++) v |= (int)((p[b] >> bit) & 1u) << b;
     return v;
 }
 
@@ -2000,7 +2005,7 @@ __device__ __forceinline__ void cp_async_wait() {
 // copies the rows of 8 of its candidate's k-mers; a step's entries load two
 // issues before its copies, and the copies kMaskStages - 1 steps before their
 // counts.
-template <int LPR>
+template <int LPR, int NP>
 __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* st,
                                                 const int32_t* __restrict__ remain,
                                                 const int32_t* s_tent, uint4* stage, int nt,
@@ -2102,11 +2107,11 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
             }
             wr = wr == kMaskStages - 1 ? 0 : wr + 1;
         };
-        uint32_t P[4][8];
+        uint32_t P[4][NP];
 #pragma unroll
         for (int w = 0; w < 4; w++)
 #pragma unroll
-            for (int b = 0; b < 8; b++) P[w][b] = 0u;
+            for (int b = 0; b < NP; b++) P[w][b] = 0u;
         uint32_t c8[4] = {0u, 0u, 0u, 0u};  // weight-8 carries of an odd step
         uint32_t en0[EPL], en1[EPL];        // entries of the next two steps to issue
         load_raw(0, en0);
@@ -2135,22 +2140,22 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
             uint4 w[8];
 #pragma unroll
             for (int u = 0; u < 8; u++) w[u] = src[32 * u];
-            const uint32_t e0 = bs_tree8(P[0], w[0].x, w[1].x, w[2].x, w[3].x, w[4].x, w[5].x, w[6].x, w[7].x);
-            const uint32_t e1 = bs_tree8(P[1], w[0].y, w[1].y, w[2].y, w[3].y, w[4].y, w[5].y, w[6].y, w[7].y);
-            const uint32_t e2 = bs_tree8(P[2], w[0].z, w[1].z, w[2].z, w[3].z, w[4].z, w[5].z, w[6].z, w[7].z);
-            const uint32_t e3 = bs_tree8(P[3], w[0].w, w[1].w, w[2].w, w[3].w, w[4].w, w[5].w, w[6].w, w[7].w);
+            const uint32_t e0 = bs_tree8<NP>(P[0], w[0].x, w[1].x, w[2].x, w[3].x, w[4].x, w[5].x, w[6].x, w[7].x);
+            const uint32_t e1 = bs_tree8<NP>(P[1], w[0].y, w[1].y, w[2].y, w[3].y, w[4].y, w[5].y, w[6].y, w[7].y);
+            const uint32_t e2 = bs_tree8<NP>(P[2], w[0].z, w[1].z, w[2].z, w[3].z, w[4].z, w[5].z, w[6].z, w[7].z);
+            const uint32_t e3 = bs_tree8<NP>(P[3], w[0].w, w[1].w, w[2].w, w[3].w, w[4].w, w[5].w, w[6].w, w[7].w);
             if (s & 1) {
-                bs_pair8(P[0], c8[0], e0);
-                bs_pair8(P[1], c8[1], e1);
-                bs_pair8(P[2], c8[2], e2);
-                bs_pair8(P[3], c8[3], e3);
+                bs_pair8<NP>(P[0], c8[0], e0);
+                bs_pair8<NP>(P[1], c8[1], e1);
+                bs_pair8<NP>(P[2], c8[2], e2);
+                bs_pair8<NP>(P[3], c8[3], e3);
             } else {
                 c8[0] = e0, c8[1] = e1, c8[2] = e2, c8[3] = e3;
             }
         }
         if (nsteps & 1) {
 #pragma unroll
-            for (int w = 0; w < 4; w++) bs_carry(P[w], 3, c8[w]);
+            for (int w = 0; w < 4; w++) bs_carry<NP>(P[w], 3, c8[w]);
         }
         // E_q over the group's lanes
 #pragma unroll
@@ -2171,11 +2176,11 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
             const uint32_t valid = ntq - t0 >= 32 ? 0xffffffffu : (1u << (ntq - t0)) - 1u;
             uint32_t hiw = 0u;
 #pragma unroll
-            for (int b = 0; b < 8; b++)
+            for (int b = 0; b < NP; b++)
                 if (b >= lb) hiw |= P[w][b];
-            if (vlo > 255 || !((vlo <= 0 ? 0xffffffffu : hiw) & valid)) continue;
-            uint32_t pass = bs_ge(P[w], cw) & valid;
-            uint32_t open = bs_ge(P[w], vlo) & valid & ~pass;
+            if (vlo > (1 << NP) - 1 || !((vlo <= 0 ? 0xffffffffu : hiw) & valid)) continue;
+            uint32_t pass = bs_ge<NP>(P[w], cw) & valid;
+            uint32_t open = bs_ge<NP>(P[w], vlo) & valid & ~pass;
             if (!(pass | open)) continue;
             if (!have_cq) {
                 cq = R.comp[q];
@@ -2197,7 +2202,7 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
                 const int b = __ffs(open) - 1;
                 open &= open - 1;
                 const int t = t0 + b;
-                if (bs_get(P[w], b) + min(tex[t], ex) < cw) continue;
+                if (bs_get<NP>(P[w], b) + min(tex[t], ex) < cw) continue;
                 mc.n_wf++;
                 const int rep = s_tent[t];
                 if (prefilter_pass(R.comp[rep], cq, cbq)) {
@@ -2213,6 +2218,7 @@ __device__ __forceinline__ void mask_candidates(const DevReads& R, RoundState* s
 
 constexpr int kMaskSmem = (kMaskThreads / 32) * kMaskStages * kMaskStepBytes;
 
+template <int NP>
 __global__ void __launch_bounds__(kMaskThreads, 2) k_bfilter_mask(
     DevReads R, RoundState* st, const int32_t* __restrict__ remain,
     const int32_t* __restrict__ tent, const uint4* __restrict__ tm4, int rwq,
@@ -2228,16 +2234,16 @@ __global__ void __launch_bounds__(kMaskThreads, 2) k_bfilter_mask(
     MaskCounts mc;
     const int quads = (nt + 127) >> 7;  // 16-byte words of the pass's rows
     if (quads > 4)
-        mask_candidates<8>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
+        mask_candidates<8, NP>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
                            amb, amb_cap, mc);
     else if (quads > 2)
-        mask_candidates<4>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
+        mask_candidates<4, NP>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
                            amb, amb_cap, mc);
     else if (quads > 1)
-        mask_candidates<2>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
+        mask_candidates<2, NP>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
                            amb, amb_cap, mc);
     else
-        mask_candidates<1>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
+        mask_candidates<1, NP>(R, st, remain, s_tent, stage, nt, n, tm4, rwq, tex, pairs, seg_cap,
                            amb, amb_cap, mc);
     const unsigned n_wf = (unsigned)warp_sum_i((int)mc.n_wf);
     const unsigned n_al = (unsigned)warp_sum_i((int)mc.n_al);
@@ -2629,18 +2635,27 @@ void launch_bfilter_bits_t(const DevReads& R, RoundBuffers& B, const int32_t* re
 template <int K>
 void launch_bfilter_mask_t(const DevReads& R, RoundBuffers& B, const int32_t* remain,
                            cudaStream_t s) {
-    static int grid = 0;
-    if (!grid) {
-        cudaFuncSetAttribute(k_bfilter_mask, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    static int grid8 = 0, grid10 = 0;
+    if (!grid8) {
+        cudaFuncSetAttribute(k_bfilter_mask<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              kMaskSmem);
-        grid = grid_for(k_bfilter_mask, kMaskThreads, kMaskSmem, 2);
+        cudaFuncSetAttribute(k_bfilter_mask<10>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kMaskSmem);
+        grid8 = grid_for(k_bfilter_mask<8>, kMaskThreads, kMaskSmem, 2);
+        grid10 = grid_for(k_bfilter_mask<10>, kMaskThreads, kMaskSmem, 2);
     }
     cudaMemsetAsync(B.tmask, 0, sizeof(uint4) * ((size_t)1 << (2 * K)) * B.tmask_rwq, s);
     k_bmask<<<kMaxBatch / 8, 256, 0, s>>>(R, B.st, B.tent, reinterpret_cast<uint32_t*>(B.tmask),
                                           B.tmask_ex, B.tmask_rwq);
-    k_bfilter_mask<<<shaped(grid, R.filter_blocks), kMaskThreads, kMaskSmem, s>>>(
-        R, B.st, remain, B.tent, B.tmask, B.tmask_rwq, B.tmask_ex, B.pairs, B.seg_cap, B.amb,
-        B.amb_cap);
+    // eight count planes where no read has more than 255 k-mer entries, else ten
+    if (B.tmask_planes <= 8)
+        k_bfilter_mask<8><<<shaped(grid8, R.filter_blocks), kMaskThreads, kMaskSmem, s>>>(
+            R, B.st, remain, B.tent, B.tmask, B.tmask_rwq, B.tmask_ex, B.pairs, B.seg_cap, B.amb,
+            B.amb_cap);
+    else
+        k_bfilter_mask<10><<<shaped(grid10, R.filter_blocks), kMaskThreads, kMaskSmem, s>>>(
+            R, B.st, remain, B.tent, B.tmask, B.tmask_rwq, B.tmask_ex, B.pairs, B.seg_cap, B.amb,
+            B.amb_cap);
     launch_exact_t<K>(R, B, s);
 }
 

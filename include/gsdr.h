@@ -52,7 +52,7 @@ typedef struct {
     int32_t word_filter;  /* batched word filter form: 0 automatic, 1 per-tentative k-mer
                              tables, 2 inverted k-mer index, 3 two-level k-mer count
                              bitmaps (k <= 7), 4 per-k-mer tentative masks (k <= 7,
-                             reads of at most 255 k-mers; otherwise the automatic
+                             reads of at most 1,023 k-mers; otherwise the automatic
                              form); the result is the same in every form */
     int32_t variant;      /* semantics: 0 = cuda-version (func.cu, the default);
                              1 = the top-level SYCL program (func.cpp): k from t by

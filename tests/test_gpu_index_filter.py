@@ -249,11 +249,19 @@ def test_masks_low_complexity_open_pairs(tmp_path, monkeypatch, t, batch):
 
 
 def test_masks_fall_back_for_long_reads(tmp_path, monkeypatch):
-    # reads above 255 k-mers: the counts would not fit the masks' 8 planes,
-    # so the forced form falls back to the automatic one
-    data = gsdr.synth_fasta(0, n_reads=1500, seed=50)
+    # reads above 1,023 k-mers: the counts would not fit the masks' ten
+    # planes, so the forced form falls back to the automatic one
+    data = gsdr.synth_fasta(1, n_reads=1500, seed=50)
     st, _ = run_form(data, tmp_path, monkeypatch, 0.95, 64, "masks")
     assert st.word_index != 3
+
+
+@pytest.mark.parametrize("w,batch", [(6, 64), (6, 1024), (7, 300), (5, 0)])
+def test_masks_ten_planes(tmp_path, monkeypatch, w, batch):
+    # 200-1000 bp reads: up to ~1,000 k-mer entries, counts in ten planes
+    data = gsdr.synth_fasta(0, n_reads=2500, seed=51)
+    st, _ = run_form(data, tmp_path, monkeypatch, 0.95, batch, "masks", w=w)
+    assert st.k == w and st.word_index == 3
 
 
 def test_masks_form_is_repeatable(monkeypatch):
