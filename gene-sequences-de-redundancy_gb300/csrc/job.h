@@ -18,8 +18,10 @@ public:
     ~Job();
     // Validates options and sizes, allocates device memory, creates the stream.
     int init(const gsdr_reads* reads, const gsdr_opts* opts, cudaStream_t stream = nullptr);
-    // Host -> device copy of the reads; with dev_bytes, the sequence bytes are
-    // copied from that device buffer instead of reads->bytes.
+    // Host -> device copy of the reads.  With dev_bytes, the job reads the
+    // sequence bytes from that device buffer in place instead of reads->bytes:
+    // its base 16-byte aligned, readable 16 bytes past reads->n_bytes, and
+    // allocated and unchanged until the job's last kernel has run.
     int upload(const gsdr_reads* reads, const void* dev_bytes = nullptr);
     // Device views for kernels that follow the clustering (output formatting).
     const DevReads& device_reads() const { return R_; }
