@@ -590,7 +590,10 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     // (the record lengths are below 2^31, so comparing them as 64-bit values
     // gives the comparator's outcomes, hence the permutation, of 32-bit ones)
     const int64_t* dlp = h_dlen;
-    std::vector<int64_t> s_off(nr);
+    // (kept per thread between calls: a fresh array costs page faults and a
+    // zero fill; every entry is written by the gather)
+    static thread_local std::vector<int64_t> s_off;
+    s_off.resize(nr);
     res->length.resize(nr);
     // offsets and lengths in sorted order, gathered by the sort's own threads
     // (one thread takes ~1 ms for the 200k-read workload: random reads of
