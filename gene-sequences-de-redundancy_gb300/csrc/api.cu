@@ -39,8 +39,6 @@ double now_ms() {
 
 namespace {
 
-inline int64_t round4(int64_t v) { return (v + 3) & ~(int64_t)3; }
-
 int cuda_fail(cudaError_t e, const char* what) {
     std::string m = std::string(what) + ": " + cudaGetErrorString(e);
     return fail(e == cudaErrorMemoryAllocation ? GSDR_ENOMEM : GSDR_EDEVICE, m.c_str());
@@ -64,28 +62,8 @@ struct Carve {
     }
 };
 
-// The per-read offset arrays of the jobs a thread sets up, kept between
-// jobs: a fresh pair of arrays per job (2 x 1.6 MB for the 200k-read
-// workload) costs page faults and a zero fill on every job.
-struct OffsetCache {
-    std::vector<int64_t> pack_off, kmer_off;
-};
-thread_local OffsetCache t_offsets;
-
-void give_offsets(std::vector<int64_t>& pack_off, std::vector<int64_t>& kmer_off) {
-    if (pack_off.capacity() > t_offsets.pack_off.capacity()) pack_off.swap(t_offsets.pack_off);
-    if (kmer_off.capacity() > t_offsets.kmer_off.capacity()) kmer_off.swap(t_offsets.kmer_off);
-}
-
 // Layout plan shared by footprint() and plan_and_alloc().
 struct Plan {
-    Plan() {
-        pack_off.swap(t_offsets.pack_off);
-        kmer_off.swap(t_offsets.kmer_off);
-    }
-    ~Plan() { give_offsets(pack_off, kmer_off); }
-    Plan(const Plan&) = delete;
-    Plan& operator=(const Plan&) = delete;
     std::vector<int64_t> pack_off, kmer_off;
     int64_t max_len = 0;
     int r_max = 1;          // largest R (tentatives per pass)
@@ -115,43 +93,42 @@ int job_r_max(const gsdr_opts& o) {
 // k-mers.  GSDR_BFILTER=table|index|bits|masks forces a form.
 constexpr int64_t kIndexDensity = 8;
 
-int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P) {
+int make_plan(const gsdr_reads* reads, const gsdr_opts& o, Plan& P, PlanPreset* pre) {
     const int n = reads->n;
     const bool drop = o.drop == 1;
     const int k = o.word_length;
-    // (every entry past the first is written below)
-    P.pack_off.resize(n + 1);
-    P.kmer_off.resize(n + 1);
-    P.pack_off[0] = 0;
-    P.kmer_off[0] = 0;
     P.variant = o.variant;
     P.r_max = (o.batch == 1 || (!drop && k >= kWideK)) ? 1 : job_r_max(o);
     const int64_t kcap = (int64_t)1 << (2 * (k > 0 ? k : 1));
-    int64_t ents_sum = 0, ents_max = 0, pack_run = 0, kmer_run = 0;
+    // the per-read layout (plan_chunks.h): the caller's, when it computed it
+    // for these options and every read was in range, else one pass here
+    PlanChunk sums;
+    if (pre && pre->k == k && pre->drop == drop && pre->sums.valid &&
+        pre->pack_off.size() == (size_t)n + 1 && pre->kmer_off.size() == (size_t)n + 1) {
+        P.pack_off.swap(pre->pack_off);
+        P.kmer_off.swap(pre->kmer_off);
+        sums = pre->sums;
+    } else {
+        P.pack_off.assign(n + 1, 0);
+        P.kmer_off.assign(n + 1, 0);
+        sums = plan_chunk(reads->offset, reads->length, reads->n_bytes, 0, n, k, drop,
+                          P.pack_off.data(), P.kmer_off.data());
+        if (!sums.valid)
+            for (int i = 0; i < n; i++) {
+                const int64_t L = reads->length[i];
+                if (L < 0) return fail(GSDR_EINVAL, "negative read length");
+                if (reads->offset[i] < 0 || reads->offset[i] + L > reads->n_bytes)
+                    return fail(GSDR_EINVAL, "read outside the byte buffer");
+            }
+    }
+    P.max_len = sums.max_len;
+    const int64_t ents_sum = sums.ents_sum, ents_max = sums.ents_max;
+    const bool sorted = sums.sorted;
     std::vector<int64_t> head;  // entries of the first kMaxBatch reads, prefix sums
     head.reserve(kMaxBatch + 1);
     head.push_back(0);
-    bool sorted = true;
-    for (int i = 0; i < n; i++) {
-        const int64_t L = reads->length[i];
-        if (L < 0) return fail(GSDR_EINVAL, "negative read length");
-        if (reads->offset[i] < 0 || reads->offset[i] + L > reads->n_bytes)
-            return fail(GSDR_EINVAL, "read outside the byte buffer");
-        if (L > P.max_len) P.max_len = L;
-        if (i > 0 && L > reads->length[i - 1]) sorted = false;
-        // (the running offsets stay in registers: reading back the entry just
-        // stored would chain every iteration on a store-to-load forward)
-        pack_run += round4(L / 16 + 1);
-        P.pack_off[i + 1] = pack_run;
-        int64_t ents = drop ? 0 : L - k + 1;
-        if (ents < 0) ents = 0;
-        if (ents > kcap) ents = kcap;
-        ents_sum += ents;
-        if (ents > ents_max) ents_max = ents;
-        if (i < kMaxBatch) head.push_back(head.back() + ents);
-        kmer_run += round4(ents);
-        P.kmer_off[i + 1] = kmer_run;
-    }
+    for (int i = 0; i < n && i < kMaxBatch; i++)
+        head.push_back(head.back() + plan_entries(reads->length[i], k, drop));
     if (o.pigeon == 1 && !drop) {
         P.refoff16.resize(n);
         int64_t ro = 0;
@@ -331,21 +308,21 @@ Job::~Job() {
     pinned_release(h_done_);
     pinned_release(h_state_);
     if (own_stream_ && stream) cudaStreamDestroy(stream);
-    give_offsets(pack_off_, kmer_off_);
 }
 
 int64_t Job::footprint(const gsdr_reads* reads, const gsdr_opts* opts) {
     gsdr_opts o;
     if (validate(reads, opts, o)) return -1;
     Plan P;
-    if (make_plan(reads, o, P)) return -1;
+    if (make_plan(reads, o, P, nullptr)) return -1;
     DevReads R{};
     RoundBuffers B{};
     return (int64_t)carve_all(nullptr, reads->n, reads->n_bytes, P, o.drop == 1, o.word_length,
                               R, B);
 }
 
-int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s) {
+int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s,
+               PlanPreset* preset) {
     const double t_start = now_ms();
     int rc = validate(reads, opts_in, opts);
     if (rc) return rc;
@@ -373,7 +350,7 @@ int Job::init(const gsdr_reads* reads, const gsdr_opts* opts_in, cudaStream_t s)
                      opts.batch, opts.word_filter, opts.group_words, opts.band_serial,
                      opts.align_blocks, opts.filter_blocks, opts.graph_steps);
     Plan P;
-    rc = make_plan(reads, opts, P);
+    rc = make_plan(reads, opts, P, preset);
     if (rc) return rc;
     const double t_plan = now_ms();
     // A read with 65,536 or more k-mers can reach a word-filter sum of 65,536,

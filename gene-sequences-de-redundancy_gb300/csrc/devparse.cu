@@ -21,12 +21,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <new>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gsdr.h"
@@ -597,21 +599,66 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
     res->length.resize(nr);
     // offsets and lengths in sorted order, gathered by the sort's own threads
     // (one thread takes ~1 ms for the 200k-read workload: random reads of
-    // arrays the copy wrote)
+    // arrays the copy wrote).  The same threads then lay out the job over the
+    // reads each gathered (plan_chunks.h), so that Job::init skips its serial
+    // pass over all reads (0.5 ms for the 200k-read workload).
     const int32_t* ord = res->order.data();
     const int64_t* doff = h_doff;
     int64_t* soff = s_off.data();
     int32_t* slen = res->length.data();
+    const int n_threads = sort_threads();
+    const int64_t view_bytes = n + 16 + extra;
+    PlanPreset preset;
+    preset.k = o.word_length;
+    preset.drop = o.drop == 1;
+    preset.pack_off.resize((size_t)nr + 1);
+    preset.kmer_off.resize((size_t)nr + 1);
+    preset.pack_off[0] = 0;
+    preset.kmer_off[0] = 0;
+    std::vector<PlanChunk> parts((size_t)std::max(n_threads, 1));
+    std::atomic<int> arrived{0};
+    int used = 0;  // threads that ran the gather (set by thread 0)
+    int64_t* pk = preset.pack_off.data();
+    int64_t* km = preset.kmer_off.data();
+    PlanChunk* pp = parts.data();
+    std::atomic<int>* arr = &arrived;
+    int* usedp = &used;
+    const int k_plan = preset.k;
+    const bool drop_plan = preset.drop;
     const std::function<void(int, int)> gather = [=](int t, int T) {
         const int32_t lo = (int32_t)((int64_t)nr * t / T), hi = (int32_t)((int64_t)nr * (t + 1) / T);
         for (int32_t i = lo; i < hi; i++) {
             soff[i] = doff[ord[i]];
             slen[i] = (int32_t)dlp[ord[i]];
         }
+        pp[t] = plan_chunk(soff, slen, view_bytes, lo, hi, k_plan, drop_plan, pk, km);
+        // all T threads run this callback at once (stdsort.h): wait for the
+        // others' sums, then add those of the parts before this one
+        arr->fetch_add(1, std::memory_order_acq_rel);
+        while (arr->load(std::memory_order_acquire) < T) std::this_thread::yield();
+        int64_t pack_base = 0, kmer_base = 0;
+        for (int u = 0; u < t; u++) {
+            pack_base += pp[u].pack;
+            kmer_base += pp[u].kmer;
+        }
+        plan_shift(lo, hi, pack_base, kmer_base, pk, km);
+        if (t == 0) *usedp = T;
     };
     std_sort_threaded(res->order.begin(), res->order.end(),
                       [dlp](const int32_t& a, const int32_t& c) { return dlp[a] > dlp[c]; },
-                      sort_threads(), gather);
+                      n_threads, gather);
+    if (used > 0 && used <= (int)parts.size()) {
+        PlanChunk all = parts[0];
+        for (int u = 1; u < used; u++) {
+            const int32_t lo = (int32_t)((int64_t)nr * u / used);
+            const int32_t hi = (int32_t)((int64_t)nr * (u + 1) / used);
+            const bool follows = lo >= hi || lo == 0 || slen[lo] <= slen[lo - 1];
+            all = plan_join(all, parts[u], follows);
+        }
+        preset.sums = all;
+    } else {
+        preset.k = -1;  // not laid out: Job::init takes its own pass
+    }
     const double t_parse = now_ms();
     mark("sort");
     range_read.end();
@@ -629,7 +676,7 @@ int cluster_fasta(const char* fasta, int64_t n, const gsdr_opts* opts_in, gsdr_r
         if (rc) return rc;
     }
     Job job;
-    rc = job.init(&view, &o, s);
+    rc = job.init(&view, &o, s, &preset);
     mark("job_init");
     if (!rc) rc = job.upload(&view, b);
     mark("upload");

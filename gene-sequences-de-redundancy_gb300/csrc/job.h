@@ -10,6 +10,7 @@
 
 #include "gsdr.h"
 #include "gsdr_device.cuh"
+#include "plan_chunks.h"
 
 namespace gsdr {
 
@@ -17,7 +18,10 @@ class Job {
 public:
     ~Job();
     // Validates options and sizes, allocates device memory, creates the stream.
-    int init(const gsdr_reads* reads, const gsdr_opts* opts, cudaStream_t stream = nullptr);
+    // preset: the reads' layout, computed by the caller for the resolved word
+    // length and drop mode (plan_chunks.h); init takes its arrays.
+    int init(const gsdr_reads* reads, const gsdr_opts* opts, cudaStream_t stream = nullptr,
+             PlanPreset* preset = nullptr);
     // Host -> device copy of the reads.  With dev_bytes, the job reads the
     // sequence bytes from that device buffer in place instead of reads->bytes:
     // its base 16-byte aligned, readable 16 bytes past reads->n_bytes, and
