@@ -1,7 +1,8 @@
 // gsdr_device.cuh -- device-side data layout and kernel entry points.
 //
 // Layout in HBM of one clustering job (n reads in length-sorted order):
-//   raw bytes    the caller's sequence bytes, one H2D copy, read i at offset[i]
+//   raw bytes    the caller's sequence bytes, one H2D copy (or the FASTA
+//                path's device copy of the file, read in place), read i at offset[i]
 //   len, len_gf  raw length (with gaps) and gap-free length       i32[n]
 //   pack_off     word offset of read i in `packed` (multiple of 4) i64[n+1]
 //   packed       2-bit codes, 16 bases per u32, first base in bits 31:30
